@@ -161,12 +161,14 @@ def main():
     lines.append('#define RYS_DEG %d' % DEG)
     lines.append('#define RYS_WIDTH %d' % WIDTH)
     nint = [0] + [t_asym(n) // WIDTH for n in range(1, NMAX + 1)]
-    offs = [0]
-    for n in range(1, NMAX + 1):
+    # offs[n] = first element of the block for n roots (offs[0] unused)
+    offs = [0, 0]
+    for n in range(1, NMAX):
         offs.append(offs[-1] + nint[n] * (DEG + 1) * 2 * n)
-    lines.append('#define RYS_TABLE_SIZE %d' % offs[-1])
+    total = offs[-1] + nint[NMAX] * (DEG + 1) * 2 * NMAX
+    lines.append('#define RYS_TABLE_SIZE %d' % total)
     lines.append('static const int rys_nint_host[RYS_NMAX + 1] = {%s};' % ', '.join(map(str, nint)))
-    lines.append('static const int rys_offset_host[RYS_NMAX + 1] = {%s};' % ', '.join(map(str, offs[:-1])))
+    lines.append('static const int rys_offset_host[RYS_NMAX + 1] = {%s};' % ', '.join(map(str, offs)))
     lines.append('// layout per n: [interval][power 0..DEG][u_1..u_n, w_1..w_n]')
     lines.append('static const double rys_coef_host[RYS_TABLE_SIZE] = {')
     for n in range(1, NMAX + 1):
@@ -181,8 +183,11 @@ def main():
         hx.extend(float(v * v) for v in x[n:])
         hw.extend(float(v) for v in W[n:])
     lines.append('// Gauss-Hermite asymptote per n (offset n(n-1)/2): squared positive nodes and weights')
-    lines.append('static const double rys_asym_x2_host[%d] = {%s};' % (len(hx), ', '.join(float.hex(v) for v in hx)))
-    lines.append('static const double rys_asym_w_host[%d] = {%s};' % (len(hw), ', '.join(float.hex(v) for v in hw)))
+    lines.append('#define RYS_ASYM_SIZE %d' % len(hx))
+    lines.append('#define RYS_ASYM_X2_LIST %s' % ', '.join(float.hex(v) for v in hx))
+    lines.append('#define RYS_ASYM_W_LIST %s' % ', '.join(float.hex(v) for v in hw))
+    lines.append('static const double rys_asym_x2_host[RYS_ASYM_SIZE] = {RYS_ASYM_X2_LIST};')
+    lines.append('static const double rys_asym_w_host[RYS_ASYM_SIZE] = {RYS_ASYM_W_LIST};')
     out = os.path.join(os.path.dirname(os.path.abspath(__file__)), 'rys_tables.inc')
     with open(out, 'w') as f:
         f.write('\n'.join(lines) + '\n')

@@ -1,0 +1,44 @@
+// Kernel instantiations for one bra pair class, selected at compile time by
+// -DJK_BRA_CLASS=<0..9>; the build compiles this file once per bra class so
+// the translation units build in parallel.
+#include "jk_kernel.cuh"
+#include "jk_registry.h"
+
+#ifndef JK_BRA_CLASS
+#error "compile with -DJK_BRA_CLASS=<pair class>"
+#endif
+
+namespace jk {
+
+template <int LI, int LJ, int LK, int LL>
+static void reg_one(ClassEntry *tab) {
+    using S64 = ClassShape<LI, LJ, LK, LL, double>;
+    using S32 = ClassShape<LI, LJ, LK, LL, float>;
+    ClassEntry &e = tab[quartet_class(pair_class(LI, LJ), pair_class(LK, LL))];
+    e.li = LI; e.lj = LJ; e.lk = LK; e.ll = LL;
+    e.qb64 = S64::QB; e.smem64 = S64::SMEM;
+    e.qb32 = S32::QB; e.smem32 = S32::SMEM;
+    e.k64 = (const void *)rys_class_kernel<LI, LJ, LK, LL, double, MODE_JK>;
+    e.k32 = (const void *)rys_class_kernel<LI, LJ, LK, LL, float, MODE_JK>;
+    if constexpr (LI == LK && LJ == LL) {
+        e.kdiag = (const void *)rys_class_kernel<LI, LJ, LK, LL, double, MODE_DIAG>;
+        e.qbdiag = S64::QB; e.smemdiag = S64::SMEM;
+    } else {
+        e.kdiag = nullptr; e.qbdiag = 0; e.smemdiag = 0;
+    }
+}
+
+template <int A, int B>
+static void reg_kets(ClassEntry *tab) {
+    reg_one<pc_li(A), pc_lj(A), pc_li(B), pc_lj(B)>(tab);
+    if constexpr (B > 0) reg_kets<A, B - 1>(tab);
+}
+
+#define JK_CAT2(a, b) a##b
+#define JK_CAT(a, b) JK_CAT2(a, b)
+
+void JK_CAT(register_bra_class_, JK_BRA_CLASS)(ClassEntry *tab) {
+    reg_kets<JK_BRA_CLASS, JK_BRA_CLASS>(tab);
+}
+
+}  // namespace jk

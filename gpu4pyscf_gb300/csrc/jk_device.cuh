@@ -1,0 +1,110 @@
+// Device side of the GB300 Rys J/K engine: data layout shared by the host
+// driver and the per-class kernel template.
+//
+// One kernel instantiation per angular class (li,lj|lk,ll) with li>=lj,
+// lk>=ll and class(ij) >= class(kl), in FP64 or FP32.  A block of 256
+// threads works on QB shell quartets that share the bra pair; each quartet
+// is owned by G threads.  Per primitive quartet the block runs three
+// stages separated by barriers:
+//   S1  one thread per quartet: Rys roots and weights (table Horner or
+//       Gauss-Hermite asymptote), prefactor and recurrence scalars -> smem;
+//   S2  one thread per (quartet, root, axis): 2D integrals by the vertical
+//       recurrence with the bra horizontal transfer done column by column in
+//       registers, then the ket horizontal transfer in place -> smem;
+//   S3  every thread: its slice of the Cartesian ERI block accumulates
+//       sum_r gx*gy*gz in registers.
+// After the primitive loop the block stages the contracted ERIs in shared
+// memory and forms the six J/K contractions, one output element per thread,
+// with one FP64 atomic add per element (instead of one per ERI and
+// contraction).
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#define JK_LMAX 3
+#define JK_THREADS 256
+#define JK_SMEM_CAP (100 * 1024)
+
+namespace jk {
+
+struct __align__(32) d4 { double x, y, z, w; };
+
+struct ShellDev {
+    double x, y, z;
+    int l, nprim, ao, pad;
+};
+
+// one pair class (li, lj) with pairs sorted by Schwarz factor, descending
+struct PairList {
+    int n;
+    const int2 *ij;        // shell indices (i >= j)
+    const float *logq;     // log sqrt(max |(ij|ij)|)
+    const int *prim_off;   // first primitive pair
+};
+
+struct EngineDev {
+    const ShellDev *shells;
+    // primitive-pair data, one entry per primitive pair of every kept shell pair
+    const d4 *pp_a;        // {p, Px, Py, Pz}
+    const d4 *pp_b;        // {PAx, PAy, PAz, Kab*ci*cj}   (A = first shell)
+    const double *pp_ip;      // 1/p
+    const float4 *pp_af;      // float copies for the FP32 quartets
+    const float4 *pp_bf;
+    const float *pp_ipf;
+    const float *dm_cond;     // [nbas*nbas] log absmax of the density blocks
+    const double *rys_coef;   // Rys interpolation table
+    const float *rys_coef_f;
+    const double *dmj;        // [n_dm][nao][nao]  D + D^T
+    const double *dmk;        // [n_dmk][nao][nao] densities for K
+    const float *dmj_f;       // float copies (FP32 quartets)
+    const float *dmk_f;
+    double *vj;               // J accumulator, symmetrised later
+    double *vk;               // K accumulator
+    float *qout;              // Schwarz mode output (per pair)
+    unsigned long long *counters;  // per class: [quartets, prim quartets]
+    int nbas, nao, n_dm, n_dmk;
+    int with_j, with_k;
+    float log_cut;
+};
+
+struct ClassDev {
+    PairList bra, ket;
+    int same;                 // bra list == ket list
+    int class_id;
+    const int *tile_off;      // [bra.n + 1] prefix of tiles per bra pair
+    const int *ket_begin;     // [bra.n]
+    const int *ket_end;       // [bra.n]
+};
+
+__host__ __device__ constexpr int ncart(int l) { return (l + 1) * (l + 2) / 2; }
+
+// Threads per quartet and quartets per block for a class.
+template <int LI, int LJ, int LK, int LL, typename Real>
+struct ClassShape {
+    static constexpr int NFI = ncart(LI), NFJ = ncart(LJ), NFK = ncart(LK), NFL = ncart(LL);
+    static constexpr int NF = NFI * NFJ * NFK * NFL;
+    static constexpr int NR = (LI + LJ + LK + LL) / 2 + 1;
+    static constexpr int IJ = LI + LJ, KL = LK + LL;
+    static constexpr int GSKL = (LK + 1) * (LL + 1);
+    static constexpr int GS = (LI + 1) * (LJ + 1) * GSKL;   // 2D integrals per (root, axis)
+    static constexpr int NSC = 20;                            // per-quartet scalars
+    __host__ __device__ static constexpr int g_bytes(int qb) { return qb * NR * 3 * GS * (int)sizeof(Real); }
+    __host__ __device__ static constexpr int e_bytes(int qb) { return qb * NF * (int)sizeof(Real); }
+    __host__ __device__ static constexpr int aux_bytes(int qb) { return qb * (NR * 2 + NSC) * (int)sizeof(Real); }
+    __host__ __device__ static constexpr int smem_of(int g) {
+        return (g_bytes(JK_THREADS / g) > e_bytes(JK_THREADS / g) ? g_bytes(JK_THREADS / g) : e_bytes(JK_THREADS / g))
+               + aux_bytes(JK_THREADS / g);
+    }
+    __host__ __device__ static constexpr int pick_g() {
+        int g = 1;
+        while (g * 40 < NF && g < JK_THREADS) g *= 2;
+        while (smem_of(g) > JK_SMEM_CAP && g < JK_THREADS) g *= 2;
+        return g;
+    }
+    static constexpr int G = pick_g();
+    static constexpr int QB = JK_THREADS / G;
+    static constexpr int NPT = (NF + G - 1) / G;
+    static constexpr int SMEM = smem_of(G);
+};
+
+}  // namespace jk

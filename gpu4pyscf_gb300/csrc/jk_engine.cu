@@ -1,0 +1,709 @@
+// Host driver of the GB300 J/K engine: the C ABI of include/gb300jk.h.
+//
+//   jk_opt_create: shell and primitive-pair data, Schwarz factors on the GPU
+//     (diagonal quartets through the same class kernels), pruning and sorting
+//     of the shell pairs of every (li, lj) class by Schwarz factor, planning
+//     buffers.  Follows what gpu4pyscf's _VHFOpt.build and
+//     _cache_q_cond_and_non0pairs prepare (gpu4pyscf/scf/jk.py:423-442,
+//     984-1120), in this engine's own layout.
+//   jk_build: densities -> screening table -> per-class work ranges (all on
+//     the device, no host synchronisation) -> one launch per angular class
+//     and precision -> symmetrisation into the caller's buffers.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <mutex>
+#include <numeric>
+#include <string>
+#include <vector>
+
+#include "../../include/gb300jk.h"
+#include "jk_device.cuh"
+#include "jk_registry.h"
+#include "rys_tables.inc"
+
+using namespace jk;
+
+namespace {
+
+thread_local std::string g_last_error;
+
+int fail(int code, const std::string &msg) {
+    g_last_error = msg;
+    return code;
+}
+
+#define CK(call)                                                                         \
+    do {                                                                                 \
+        cudaError_t e_ = (call);                                                         \
+        if (e_ != cudaSuccess)                                                           \
+            return fail(JK_ERR_CUDA, std::string(#call) + ": " + cudaGetErrorString(e_)); \
+    } while (0)
+
+ClassEntry g_tab[NQCLASS];
+std::once_flag g_tab_once;
+
+void init_registry() {
+    std::memset(g_tab, 0, sizeof(g_tab));
+    register_bra_class_0(g_tab);
+    register_bra_class_1(g_tab);
+    register_bra_class_2(g_tab);
+    register_bra_class_3(g_tab);
+    register_bra_class_4(g_tab);
+    register_bra_class_5(g_tab);
+    register_bra_class_6(g_tab);
+    register_bra_class_7(g_tab);
+    register_bra_class_8(g_tab);
+    register_bra_class_9(g_tab);
+}
+
+template <typename T>
+int dalloc(T **p, size_t n) {
+    *p = nullptr;
+    if (n == 0) n = 1;
+    cudaError_t e = cudaMalloc((void **)p, n * sizeof(T));
+    if (e != cudaSuccess) return fail(JK_ERR_ALLOC, std::string("cudaMalloc: ") + cudaGetErrorString(e));
+    return 0;
+}
+
+template <typename T>
+int upload(T **p, const std::vector<T> &h) {
+    int err = dalloc(p, h.size());
+    if (err) return err;
+    if (!h.empty()) {
+        cudaError_t e = cudaMemcpy(*p, h.data(), h.size() * sizeof(T), cudaMemcpyHostToDevice);
+        if (e != cudaSuccess) return fail(JK_ERR_CUDA, std::string("cudaMemcpy: ") + cudaGetErrorString(e));
+    }
+    return 0;
+}
+
+inline int ncart_h(int l) { return (l + 1) * (l + 2) / 2; }
+
+// ---------------------------------------------------------------------------
+// small device kernels: densities, screening table, planning, epilogue
+// ---------------------------------------------------------------------------
+
+__global__ void prep_dm_kernel(const double *dm, int n_dm, int nao, int hermi, int mixed,
+                               double *dmj, double *dmk, float *dmj_f, float *dmk_f) {
+    size_t nn = (size_t)nao * nao;
+    size_t total = nn * n_dm;
+    for (size_t x = blockIdx.x * (size_t)blockDim.x + threadIdx.x; x < total; x += (size_t)gridDim.x * blockDim.x) {
+        size_t idm = x / nn, r = x % nn;
+        size_t i = r / nao, j = r % nao;
+        double a = dm[x], at = dm[idm * nn + j * nao + i];
+        double js = a + at;
+        dmj[x] = js;
+        dmk[x] = a;
+        if (hermi == 0) dmk[(n_dm + idm) * nn + r] = at;
+        if (mixed) {
+            dmj_f[x] = (float)js;
+            dmk_f[x] = (float)a;
+            if (hermi == 0) dmk_f[(n_dm + idm) * nn + r] = (float)at;
+        }
+    }
+}
+
+__global__ void dm_cond_kernel(const double *dm, int n_dm, int nao, const ShellDev *sh, int nbas,
+                               int hermi, float *dm_cond) {
+    int ij = blockIdx.x * blockDim.x + threadIdx.x;
+    if (ij >= nbas * nbas) return;
+    int i = ij / nbas, j = ij % nbas;
+    int ni = (sh[i].l + 1) * (sh[i].l + 2) / 2, nj = (sh[j].l + 1) * (sh[j].l + 2) / 2;
+    size_t nn = (size_t)nao * nao;
+    double mij = 0., mji = 0.;
+    for (int d = 0; d < n_dm; ++d)
+        for (int a = 0; a < ni; ++a)
+            for (int b = 0; b < nj; ++b) {
+                mij = fmax(mij, fabs(dm[d * nn + (size_t)(sh[i].ao + a) * nao + sh[j].ao + b]));
+                mji = fmax(mji, fabs(dm[d * nn + (size_t)(sh[j].ao + b) * nao + sh[i].ao + a]));
+            }
+    double v = hermi == 0 ? mij + mji : fmax(mij, mji);
+    dm_cond[ij] = (float)log(v + 1e-300);
+}
+
+__global__ void max_kernel(const float *x, int n, float *out) {
+    __shared__ float red[1024];
+    float m = -1e30f;
+    for (int i = threadIdx.x; i < n; i += blockDim.x) m = fmaxf(m, x[i]);
+    red[threadIdx.x] = m;
+    __syncthreads();
+    for (int s = blockDim.x / 2; s > 0; s >>= 1) {
+        if (threadIdx.x < s) red[threadIdx.x] = fmaxf(red[threadIdx.x], red[threadIdx.x + s]);
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) out[0] = red[0];
+}
+
+struct PlanClass {
+    const float *bra_logq;
+    const float *ket_logq;
+    int nbra, nket, same, qb64, qb32;
+    int *kb64, *ke64, *cnt64, *kb32, *ke32, *cnt32;
+    int bra_start;  // offset in the flattened bra index space
+};
+
+// number of entries of the descending array q[0..n) with q[k] >= thr
+__device__ int count_ge(const float *q, int n, float thr) {
+    int lo = 0, hi = n;
+    while (lo < hi) {
+        int mid = (lo + hi) >> 1;
+        if (q[mid] >= thr) lo = mid + 1; else hi = mid;
+    }
+    return lo;
+}
+
+__global__ void plan_kernel(const PlanClass *pcs, int npc, int total, const float *dm_max,
+                            float log_cut, float log_split, int mixed) {
+    int x = blockIdx.x * blockDim.x + threadIdx.x;
+    if (x >= total) return;
+    int lo = 0, hi = npc;
+    while (hi - lo > 1) {
+        int mid = (lo + hi) >> 1;
+        if (pcs[mid].bra_start <= x) lo = mid; else hi = mid;
+    }
+    const PlanClass &p = pcs[lo];
+    int ib = x - p.bra_start;
+    if (ib >= p.nbra) return;
+    float base = p.bra_logq[ib] + dm_max[0];
+    int nk = count_ge(p.ket_logq, p.nket, log_cut - base);
+    if (p.same) nk = min(nk, ib + 1);
+    int n64 = nk;
+    if (mixed) n64 = min(nk, count_ge(p.ket_logq, p.nket, log_split - base));
+    p.kb64[ib] = 0;
+    p.ke64[ib] = n64;
+    p.cnt64[ib] = (n64 + p.qb64 - 1) / p.qb64;
+    p.kb32[ib] = n64;
+    p.ke32[ib] = nk;
+    p.cnt32[ib] = mixed ? (nk - n64 + p.qb32 - 1) / p.qb32 : 0;
+}
+
+struct ScanJob { const int *cnt; int *off; int n; };
+
+// exclusive prefix sum, one block per job; off[n] = total
+__global__ void scan_kernel(const ScanJob *jobs) {
+    const ScanJob jb = jobs[blockIdx.x];
+    __shared__ int buf[1024];
+    __shared__ int carry;
+    if (threadIdx.x == 0) carry = 0;
+    __syncthreads();
+    for (int base = 0; base < jb.n; base += 1024) {
+        int i = base + threadIdx.x;
+        int v = i < jb.n ? jb.cnt[i] : 0;
+        buf[threadIdx.x] = v;
+        __syncthreads();
+        for (int s = 1; s < 1024; s <<= 1) {
+            int t = threadIdx.x >= s ? buf[threadIdx.x - s] : 0;
+            __syncthreads();
+            buf[threadIdx.x] += t;
+            __syncthreads();
+        }
+        if (i < jb.n) jb.off[i] = carry + buf[threadIdx.x] - v;
+        __syncthreads();
+        if (threadIdx.x == 1023) carry += buf[1023];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) jb.off[jb.n] = carry;
+}
+
+__global__ void epilogue_kernel(const double *jt, const double *kt, int n_dm, int nao, int hermi,
+                                int with_j, int with_k, double *vj, double *vk) {
+    size_t nn = (size_t)nao * nao;
+    size_t total = nn * n_dm;
+    for (size_t x = blockIdx.x * (size_t)blockDim.x + threadIdx.x; x < total; x += (size_t)gridDim.x * blockDim.x) {
+        size_t idm = x / nn, r = x % nn;
+        size_t i = r / nao, j = r % nao;
+        size_t xt = idm * nn + j * nao + i;
+        if (with_j) vj[x] = hermi == 2 ? 0. : jt[x] + jt[xt];
+        if (with_k) {
+            if (hermi == 1) vk[x] = kt[x] + kt[xt];
+            else if (hermi == 2) vk[x] = kt[x] - kt[xt];
+            else vk[x] = kt[x] + kt[(n_dm + idm) * nn + j * nao + i];
+        }
+    }
+}
+
+}  // namespace
+
+// ---------------------------------------------------------------------------
+// optimizer object
+// ---------------------------------------------------------------------------
+
+struct HostPairList {
+    std::vector<int2> ij;
+    std::vector<float> logq;
+    std::vector<int> prim_off;
+};
+
+struct jk_opt {
+    int device = 0;
+    int sm_count = 0;
+    int nbas = 0, nao = 0;
+    double tol = 1e-13;
+    std::vector<ShellDev> shells_h;
+    std::vector<double> exps_h, coefs_h;  // per shell primitive data
+    std::vector<int> prim0_h;              // first primitive of each shell
+    ShellDev *shells = nullptr;
+    d4 *pp_a = nullptr, *pp_b = nullptr;
+    double *pp_ip = nullptr;
+    float4 *pp_af = nullptr, *pp_bf = nullptr;
+    float *pp_ipf = nullptr;
+    double *rys_coef = nullptr;
+    float *rys_coef_f = nullptr;
+    // sorted pair lists per pair class
+    int npairs[NPAIRCLASS] = {0};
+    int2 *pl_ij[NPAIRCLASS] = {nullptr};
+    float *pl_logq[NPAIRCLASS] = {nullptr};
+    int *pl_prim[NPAIRCLASS] = {nullptr};
+    std::vector<double> qcond_h;  // [nbas*nbas]
+    // planning buffers per quartet class
+    int *kb64[NQCLASS] = {nullptr}, *ke64[NQCLASS] = {nullptr}, *cnt64[NQCLASS] = {nullptr}, *off64[NQCLASS] = {nullptr};
+    int *kb32[NQCLASS] = {nullptr}, *ke32[NQCLASS] = {nullptr}, *cnt32[NQCLASS] = {nullptr}, *off32[NQCLASS] = {nullptr};
+    PlanClass *plan_dev = nullptr;
+    ScanJob *scan_dev = nullptr;
+    int nplan = 0, nscan = 0, plan_total = 0;
+    std::vector<int> plan_classes;  // quartet classes with work
+    // workspace
+    float *dm_cond = nullptr, *dm_max = nullptr;
+    int ws_ndm = 0;
+    double *dmj = nullptr, *dmk = nullptr, *jt = nullptr, *kt = nullptr;
+    float *dmj_f = nullptr, *dmk_f = nullptr;
+    unsigned long long *counters = nullptr;
+    std::vector<void *> owned;
+};
+
+namespace {
+
+void free_all(jk_opt *o) {
+    for (void *p : o->owned) cudaFree(p);
+    o->owned.clear();
+}
+
+template <typename T>
+int own_alloc(jk_opt *o, T **p, size_t n) {
+    int e = dalloc(p, n);
+    if (!e) o->owned.push_back((void *)*p);
+    return e;
+}
+
+template <typename T>
+int own_upload(jk_opt *o, T **p, const std::vector<T> &h) {
+    int e = upload(p, h);
+    if (!e) o->owned.push_back((void *)*p);
+    return e;
+}
+
+struct PrimPairHost {
+    std::vector<d4> a, b;
+    std::vector<double> ip;
+};
+
+void add_prim_pairs(const jk_opt *o, int i, int j, PrimPairHost &pp) {
+    const ShellDev &A = o->shells_h[i], &B = o->shells_h[j];
+    double AB2 = (A.x - B.x) * (A.x - B.x) + (A.y - B.y) * (A.y - B.y) + (A.z - B.z) * (A.z - B.z);
+    for (int pa = 0; pa < A.nprim; ++pa)
+        for (int pb = 0; pb < B.nprim; ++pb) {
+            double a = o->exps_h[o->prim0_h[i] + pa], b = o->exps_h[o->prim0_h[j] + pb];
+            double ca = o->coefs_h[o->prim0_h[i] + pa], cb = o->coefs_h[o->prim0_h[j] + pb];
+            double p = a + b;
+            double K = std::exp(-a * b / p * AB2) * ca * cb;
+            double Px = (a * A.x + b * B.x) / p, Py = (a * A.y + b * B.y) / p, Pz = (a * A.z + b * B.z) / p;
+            pp.a.push_back(d4{p, Px, Py, Pz});
+            pp.b.push_back(d4{Px - A.x, Py - A.y, Pz - A.z, K});
+            pp.ip.push_back(1.0 / p);
+        }
+}
+
+int launch_class(const void *func, int grid, int smem, const EngineDev &d, const ClassDev &c, int ntiles,
+                 cudaStream_t st) {
+    void *args[] = {(void *)&d, (void *)&c, (void *)&ntiles};
+    CK(cudaLaunchKernel(func, dim3(grid), dim3(JK_THREADS), args, (size_t)smem, st));
+    return 0;
+}
+
+int set_smem_attrs() {
+    for (int q = 0; q < NQCLASS; ++q) {
+        const ClassEntry &e = g_tab[q];
+        if (e.k64) CK(cudaFuncSetAttribute(e.k64, cudaFuncAttributeMaxDynamicSharedMemorySize, e.smem64));
+        if (e.k32) CK(cudaFuncSetAttribute(e.k32, cudaFuncAttributeMaxDynamicSharedMemorySize, e.smem32));
+        if (e.kdiag) CK(cudaFuncSetAttribute(e.kdiag, cudaFuncAttributeMaxDynamicSharedMemorySize, e.smemdiag));
+    }
+    return 0;
+}
+
+EngineDev base_engine(const jk_opt *o) {
+    EngineDev d;
+    std::memset(&d, 0, sizeof(d));
+    d.shells = o->shells;
+    d.pp_a = o->pp_a; d.pp_b = o->pp_b; d.pp_ip = o->pp_ip;
+    d.pp_af = o->pp_af; d.pp_bf = o->pp_bf; d.pp_ipf = o->pp_ipf;
+    d.rys_coef = o->rys_coef; d.rys_coef_f = o->rys_coef_f;
+    d.nbas = o->nbas; d.nao = o->nao;
+    return d;
+}
+
+int grid_for(const jk_opt *o, long long upper_tiles) {
+    long long g = (long long)o->sm_count * 2;
+    if (upper_tiles < g) g = upper_tiles;
+    return (int)std::max<long long>(g, 1);
+}
+
+}  // namespace
+
+// Algorithmic FLOP model of one angular class: per primitive quartet
+// n*(3*nf + 9*g) for the recurrences and the gx*gy*gz products plus
+// C_root(n) = 52*n + 30 for the roots, weights and prefactors; per contracted
+// quartet 12*nf*n_dm for the six density contractions.
+static int64_t jk_flop_model(int li, int lj, int lk, int ll, int64_t nquart, int64_t nprim, int n_dm) {
+    int n = (li + lj + lk + ll) / 2 + 1;
+    int64_t nf = (int64_t)ncart_h(li) * ncart_h(lj) * ncart_h(lk) * ncart_h(ll);
+    int64_t g = (int64_t)(li + 1) * (lj + 1) * (lk + 1) * (ll + 1);
+    return nprim * (n * (3 * nf + 9 * g) + 52 * n + 30) + nquart * 12 * nf * n_dm;
+}
+
+extern "C" {
+
+const char *jk_last_error(void) { return g_last_error.c_str(); }
+
+int jk_opt_nao(const jk_opt *opt) { return opt ? opt->nao : -1; }
+
+int jk_opt_npairs(const jk_opt *opt) {
+    if (!opt) return -1;
+    int n = 0;
+    for (int c = 0; c < NPAIRCLASS; ++c) n += opt->npairs[c];
+    return n;
+}
+
+int jk_opt_get_qcond(const jk_opt *opt, double *q) {
+    if (!opt || !q) return fail(JK_ERR_ARG, "null argument");
+    std::memcpy(q, opt->qcond_h.data(), sizeof(double) * opt->qcond_h.size());
+    return 0;
+}
+
+void jk_opt_destroy(jk_opt *opt) {
+    if (!opt) return;
+    free_all(opt);
+    delete opt;
+}
+
+int jk_opt_create(const int32_t *atm, int natm, const int32_t *bas, int nbas, const double *env, int nenv,
+                  double tol, int flags, jk_opt **out) {
+    (void)flags;
+    if (!atm || !bas || !env || !out || natm <= 0 || nbas <= 0 || nenv <= 0 || !(tol >= 0))
+        return fail(JK_ERR_ARG, "jk_opt_create: invalid arguments");
+    std::call_once(g_tab_once, init_registry);
+    jk_opt *o = new jk_opt();
+    *out = nullptr;
+    auto bail = [&](int code) { free_all(o); delete o; return code; };
+    CK(cudaGetDevice(&o->device));
+    CK(cudaDeviceGetAttribute(&o->sm_count, cudaDevAttrMultiProcessorCount, o->device));
+    if (int e = set_smem_attrs()) return bail(e);
+    o->nbas = nbas;
+    o->tol = tol;
+    int ao = 0, prev_l = -1;
+    for (int i = 0; i < nbas; ++i) {
+        const int32_t *b = bas + 8 * i;
+        int ia = b[0], l = b[1], np = b[2], nctr = b[3], pe = b[5], pc = b[6];
+        if (ia < 0 || ia >= natm) return bail(fail(JK_ERR_ARG, "shell atom index out of range"));
+        if (l < 0 || l > JK_LMAX) return bail(fail(JK_ERR_LMAX, "shell angular momentum above the GPU limit (f)"));
+        if (nctr != 1) return bail(fail(JK_ERR_ARG, "sorted basis must have one contraction per shell"));
+        if (np <= 0 || pe < 0 || pc < 0 || pe + np > nenv || pc + np > nenv)
+            return bail(fail(JK_ERR_ARG, "shell primitive data out of range"));
+        if (l < prev_l) return bail(fail(JK_ERR_ARG, "shells must be sorted by angular momentum"));
+        prev_l = l;
+        int pcoord = atm[6 * ia + 1];
+        if (pcoord < 0 || pcoord + 3 > nenv) return bail(fail(JK_ERR_ARG, "atom coordinate pointer out of range"));
+        ShellDev s;
+        s.x = env[pcoord]; s.y = env[pcoord + 1]; s.z = env[pcoord + 2];
+        if (!std::isfinite(s.x) || !std::isfinite(s.y) || !std::isfinite(s.z))
+            return bail(fail(JK_ERR_ARG, "non-finite coordinates"));
+        s.l = l; s.nprim = np; s.ao = ao; s.pad = 0;
+        ao += ncart_h(l);
+        o->prim0_h.push_back((int)o->exps_h.size());
+        for (int p = 0; p < np; ++p) {
+            if (!(env[pe + p] > 0) || !std::isfinite(env[pc + p]))
+                return bail(fail(JK_ERR_ARG, "invalid exponent or coefficient"));
+            o->exps_h.push_back(env[pe + p]);
+            o->coefs_h.push_back(env[pc + p]);
+        }
+        o->shells_h.push_back(s);
+    }
+    o->nao = ao;
+    if (int e = own_upload(o, &o->shells, o->shells_h)) return bail(e);
+    {
+        std::vector<double> t(rys_coef_host, rys_coef_host + RYS_TABLE_SIZE);
+        std::vector<float> tf(t.begin(), t.end());
+        if (int e = own_upload(o, &o->rys_coef, t)) return bail(e);
+        if (int e = own_upload(o, &o->rys_coef_f, tf)) return bail(e);
+    }
+
+    // candidate pairs per class (i >= j), skipping pairs whose every
+    // primitive product decays below exp(-60)
+    std::vector<HostPairList> cand(NPAIRCLASS);
+    PrimPairHost cpp;
+    for (int i = 0; i < nbas; ++i)
+        for (int j = 0; j <= i; ++j) {
+            const ShellDev &A = o->shells_h[i], &B = o->shells_h[j];
+            double AB2 = (A.x - B.x) * (A.x - B.x) + (A.y - B.y) * (A.y - B.y) + (A.z - B.z) * (A.z - B.z);
+            double best = 1e300;
+            for (int pa = 0; pa < A.nprim; ++pa)
+                for (int pb = 0; pb < B.nprim; ++pb) {
+                    double a = o->exps_h[o->prim0_h[i] + pa], b = o->exps_h[o->prim0_h[j] + pb];
+                    best = std::min(best, a * b / (a + b) * AB2);
+                }
+            if (best > 60.) continue;
+            int pc = pair_class(A.l, B.l);
+            cand[pc].ij.push_back(int2{i, j});
+            cand[pc].prim_off.push_back((int)cpp.a.size());
+            add_prim_pairs(o, i, j, cpp);
+        }
+    // Schwarz factors on the GPU
+    {
+        d4 *ca = nullptr, *cb = nullptr;
+        double *cip = nullptr;
+        if (int e = upload(&ca, cpp.a)) return bail(e);
+        if (int e = upload(&cb, cpp.b)) { cudaFree(ca); return bail(e); }
+        if (int e = upload(&cip, cpp.ip)) { cudaFree(ca); cudaFree(cb); return bail(e); }
+        std::vector<int2 *> dij(NPAIRCLASS, nullptr);
+        std::vector<int *> dpo(NPAIRCLASS, nullptr);
+        std::vector<float *> dq(NPAIRCLASS, nullptr);
+        int err = 0;
+        EngineDev d = base_engine(o);
+        d.pp_a = ca; d.pp_b = cb; d.pp_ip = cip;
+        for (int pc = 0; pc < NPAIRCLASS && !err; ++pc) {
+            int n = (int)cand[pc].ij.size();
+            if (n == 0) continue;
+            if ((err = upload(&dij[pc], cand[pc].ij))) break;
+            if ((err = upload(&dpo[pc], cand[pc].prim_off))) break;
+            if ((err = dalloc(&dq[pc], n))) break;
+            const ClassEntry &e = g_tab[quartet_class(pc, pc)];
+            ClassDev c;
+            std::memset(&c, 0, sizeof(c));
+            c.bra.n = c.ket.n = n;
+            c.bra.ij = c.ket.ij = dij[pc];
+            c.bra.prim_off = c.ket.prim_off = dpo[pc];
+            c.same = 1;
+            c.class_id = quartet_class(pc, pc);
+            d.qout = dq[pc];
+            int ntiles = (n + e.qbdiag - 1) / e.qbdiag;
+            err = launch_class(e.kdiag, grid_for(o, ntiles), e.smemdiag, d, c, ntiles, 0);
+        }
+        if (!err) {
+            cudaError_t ce = cudaDeviceSynchronize();
+            if (ce != cudaSuccess) err = fail(JK_ERR_CUDA, std::string("Schwarz kernels: ") + cudaGetErrorString(ce));
+        }
+        std::vector<std::vector<float>> qh(NPAIRCLASS);
+        for (int pc = 0; pc < NPAIRCLASS && !err; ++pc) {
+            qh[pc].resize(cand[pc].ij.size());
+            if (!qh[pc].empty() &&
+                cudaMemcpy(qh[pc].data(), dq[pc], qh[pc].size() * sizeof(float), cudaMemcpyDeviceToHost) != cudaSuccess)
+                err = fail(JK_ERR_CUDA, "copy of Schwarz factors");
+        }
+        for (int pc = 0; pc < NPAIRCLASS; ++pc) { cudaFree(dij[pc]); cudaFree(dpo[pc]); cudaFree(dq[pc]); }
+        cudaFree(ca); cudaFree(cb); cudaFree(cip);
+        if (err) return bail(err);
+        // prune and sort
+        double qmax = 0.;
+        for (int pc = 0; pc < NPAIRCLASS; ++pc)
+            for (float v : qh[pc]) qmax = std::max(qmax, (double)v);
+        // keep a pair if it can reach tol with density blocks up to 1e4
+        double keep = tol > 0 ? tol / (std::max(qmax, 1e-300) * 1e4) : 0.;
+        o->qcond_h.assign((size_t)nbas * nbas, 0.);
+        PrimPairHost fpp;
+        for (int pc = 0; pc < NPAIRCLASS; ++pc) {
+            std::vector<int> idx;
+            for (int k = 0; k < (int)qh[pc].size(); ++k) {
+                const int2 &p = cand[pc].ij[k];
+                o->qcond_h[(size_t)p.x * nbas + p.y] = o->qcond_h[(size_t)p.y * nbas + p.x] = qh[pc][k];
+                if (qh[pc][k] > 0 && qh[pc][k] >= keep) idx.push_back(k);
+            }
+            std::stable_sort(idx.begin(), idx.end(), [&](int a, int b) { return qh[pc][a] > qh[pc][b]; });
+            HostPairList fin;
+            for (int k : idx) {
+                const int2 &p = cand[pc].ij[k];
+                fin.ij.push_back(p);
+                fin.logq.push_back(std::log(qh[pc][k]));
+                fin.prim_off.push_back((int)fpp.a.size());
+                add_prim_pairs(o, p.x, p.y, fpp);
+            }
+            o->npairs[pc] = (int)fin.ij.size();
+            if (int e = own_upload(o, &o->pl_ij[pc], fin.ij)) return bail(e);
+            if (int e = own_upload(o, &o->pl_logq[pc], fin.logq)) return bail(e);
+            if (int e = own_upload(o, &o->pl_prim[pc], fin.prim_off)) return bail(e);
+        }
+        std::vector<float4> af, bf;
+        std::vector<float> ipf;
+        for (size_t k = 0; k < fpp.a.size(); ++k) {
+            af.push_back(make_float4((float)fpp.a[k].x, (float)fpp.a[k].y, (float)fpp.a[k].z, (float)fpp.a[k].w));
+            bf.push_back(make_float4((float)fpp.b[k].x, (float)fpp.b[k].y, (float)fpp.b[k].z, (float)fpp.b[k].w));
+            ipf.push_back((float)fpp.ip[k]);
+        }
+        if (int e = own_upload(o, &o->pp_a, fpp.a)) return bail(e);
+        if (int e = own_upload(o, &o->pp_b, fpp.b)) return bail(e);
+        if (int e = own_upload(o, &o->pp_ip, fpp.ip)) return bail(e);
+        if (int e = own_upload(o, &o->pp_af, af)) return bail(e);
+        if (int e = own_upload(o, &o->pp_bf, bf)) return bail(e);
+        if (int e = own_upload(o, &o->pp_ipf, ipf)) return bail(e);
+    }
+    // planning buffers
+    std::vector<PlanClass> plan;
+    std::vector<ScanJob> scans;
+    int total = 0;
+    for (int a = 0; a < NPAIRCLASS; ++a)
+        for (int b = 0; b <= a; ++b) {
+            int q = quartet_class(a, b);
+            int nb = o->npairs[a], nk = o->npairs[b];
+            if (nb == 0 || nk == 0) continue;
+            const ClassEntry &e = g_tab[q];
+            if (int er = own_alloc(o, &o->kb64[q], nb)) return bail(er);
+            if (int er = own_alloc(o, &o->ke64[q], nb)) return bail(er);
+            if (int er = own_alloc(o, &o->cnt64[q], nb)) return bail(er);
+            if (int er = own_alloc(o, &o->off64[q], nb + 1)) return bail(er);
+            if (int er = own_alloc(o, &o->kb32[q], nb)) return bail(er);
+            if (int er = own_alloc(o, &o->ke32[q], nb)) return bail(er);
+            if (int er = own_alloc(o, &o->cnt32[q], nb)) return bail(er);
+            if (int er = own_alloc(o, &o->off32[q], nb + 1)) return bail(er);
+            PlanClass p;
+            p.bra_logq = o->pl_logq[a];
+            p.ket_logq = o->pl_logq[b];
+            p.nbra = nb; p.nket = nk; p.same = (a == b);
+            p.qb64 = e.qb64; p.qb32 = e.qb32;
+            p.kb64 = o->kb64[q]; p.ke64 = o->ke64[q]; p.cnt64 = o->cnt64[q];
+            p.kb32 = o->kb32[q]; p.ke32 = o->ke32[q]; p.cnt32 = o->cnt32[q];
+            p.bra_start = total;
+            total += nb;
+            plan.push_back(p);
+            scans.push_back(ScanJob{o->cnt64[q], o->off64[q], nb});
+            scans.push_back(ScanJob{o->cnt32[q], o->off32[q], nb});
+            o->plan_classes.push_back(q);
+        }
+    o->nplan = (int)plan.size();
+    o->nscan = (int)scans.size();
+    o->plan_total = total;
+    if (int e = own_upload(o, &o->plan_dev, plan)) return bail(e);
+    if (int e = own_upload(o, &o->scan_dev, scans)) return bail(e);
+    if (int e = own_alloc(o, &o->dm_cond, (size_t)nbas * nbas)) return bail(e);
+    if (int e = own_alloc(o, &o->dm_max, 1)) return bail(e);
+    if (int e = own_alloc(o, &o->counters, 4 * NQCLASS)) return bail(e);
+    *out = o;
+    return 0;
+}
+
+static int ensure_workspace(jk_opt *o, int n_dm) {
+    if (n_dm <= o->ws_ndm) return 0;
+    for (void *p : {(void *)o->dmj, (void *)o->dmk, (void *)o->jt, (void *)o->kt, (void *)o->dmj_f, (void *)o->dmk_f}) {
+        if (!p) continue;
+        auto it = std::find(o->owned.begin(), o->owned.end(), p);
+        if (it != o->owned.end()) o->owned.erase(it);
+        cudaFree(p);
+    }
+    size_t nn = (size_t)o->nao * o->nao;
+    if (int e = own_alloc(o, &o->dmj, nn * n_dm)) return e;
+    if (int e = own_alloc(o, &o->dmk, nn * 2 * n_dm)) return e;
+    if (int e = own_alloc(o, &o->jt, nn * n_dm)) return e;
+    if (int e = own_alloc(o, &o->kt, nn * 2 * n_dm)) return e;
+    if (int e = own_alloc(o, &o->dmj_f, nn * n_dm)) return e;
+    if (int e = own_alloc(o, &o->dmk_f, nn * 2 * n_dm)) return e;
+    o->ws_ndm = n_dm;
+    return 0;
+}
+
+int jk_build(jk_opt *o, const double *dm, int n_dm, int nao, int hermi, int with_j, int with_k, int precision,
+             double split_thresh, double *vj, double *vk, void *stream, jk_stats *stats) {
+    if (!o || !dm || n_dm <= 0 || nao != o->nao || hermi < 0 || hermi > 2 || (!with_j && !with_k))
+        return fail(JK_ERR_ARG, "jk_build: invalid arguments");
+    if ((with_j && !vj) || (with_k && !vk)) return fail(JK_ERR_ARG, "jk_build: missing output buffer");
+    if (precision != JK_PREC_FP64 && precision != JK_PREC_MIXED) return fail(JK_ERR_ARG, "jk_build: bad precision");
+    if (precision == JK_PREC_MIXED && !(split_thresh > 0)) return fail(JK_ERR_ARG, "jk_build: split_thresh must be > 0");
+    cudaStream_t st = (cudaStream_t)stream;
+    if (int e = ensure_workspace(o, n_dm)) return e;
+    const int mixed = precision == JK_PREC_MIXED;
+    const size_t nn = (size_t)nao * nao;
+    const int n_dmk = hermi == 0 ? 2 * n_dm : n_dm;
+    int launches = 0;
+    {
+        int grid = (int)std::min<size_t>((nn * n_dm + 255) / 256, (size_t)o->sm_count * 8);
+        prep_dm_kernel<<<grid, 256, 0, st>>>(dm, n_dm, nao, hermi, mixed, o->dmj, o->dmk, o->dmj_f, o->dmk_f);
+        int nb2 = o->nbas * o->nbas;
+        dm_cond_kernel<<<(nb2 + 255) / 256, 256, 0, st>>>(dm, n_dm, nao, o->shells, o->nbas, hermi, o->dm_cond);
+        max_kernel<<<1, 1024, 0, st>>>(o->dm_cond, nb2, o->dm_max);
+        launches += 3;
+    }
+    if (o->nplan > 0) {
+        float log_cut = o->tol > 0 ? (float)std::log(o->tol) : -1e30f;
+        float log_split = mixed ? (float)std::log(split_thresh) : 0.f;
+        plan_kernel<<<(o->plan_total + 255) / 256, 256, 0, st>>>(o->plan_dev, o->nplan, o->plan_total, o->dm_max,
+                                                                 log_cut, log_split, mixed);
+        scan_kernel<<<o->nscan, 1024, 0, st>>>(o->scan_dev);
+        launches += 2;
+    }
+    CK(cudaGetLastError());
+    if (with_j) CK(cudaMemsetAsync(o->jt, 0, sizeof(double) * nn * n_dm, st));
+    if (with_k) CK(cudaMemsetAsync(o->kt, 0, sizeof(double) * nn * n_dmk, st));
+    const bool want_stats = stats != nullptr;
+    if (want_stats) CK(cudaMemsetAsync(o->counters, 0, sizeof(unsigned long long) * 4 * NQCLASS, st));
+
+    EngineDev d = base_engine(o);
+    d.dm_cond = o->dm_cond;
+    d.dmj = o->dmj; d.dmk = o->dmk; d.dmj_f = o->dmj_f; d.dmk_f = o->dmk_f;
+    d.vj = o->jt; d.vk = o->kt;
+    d.n_dm = n_dm; d.n_dmk = n_dmk;
+    d.with_j = with_j && hermi != 2;
+    d.with_k = with_k;
+    d.log_cut = o->tol > 0 ? (float)std::log(o->tol) : -1e30f;
+    if (!d.with_j && !d.with_k) d.with_k = 0;
+    for (int q : o->plan_classes) {
+        const ClassEntry &e = g_tab[q];
+        int a = 0;
+        while ((a + 1) * (a + 2) / 2 <= q) ++a;
+        int b = q - a * (a + 1) / 2;
+        ClassDev c;
+        std::memset(&c, 0, sizeof(c));
+        c.bra = PairList{o->npairs[a], o->pl_ij[a], o->pl_logq[a], o->pl_prim[a]};
+        c.ket = PairList{o->npairs[b], o->pl_ij[b], o->pl_logq[b], o->pl_prim[b]};
+        c.same = a == b;
+        long long upper = (long long)o->npairs[a] * ((o->npairs[b] + e.qb64 - 1) / e.qb64);
+        if (!d.with_j && !d.with_k) break;
+        c.class_id = q;
+        d.counters = want_stats ? o->counters : nullptr;
+        c.tile_off = o->off64[q]; c.ket_begin = o->kb64[q]; c.ket_end = o->ke64[q];
+        if (int er = launch_class(e.k64, grid_for(o, upper), e.smem64, d, c, 0, st)) return er;
+        ++launches;
+        if (mixed) {
+            c.class_id = NQCLASS + q;  // FP32 counters in the second half
+            c.tile_off = o->off32[q]; c.ket_begin = o->kb32[q]; c.ket_end = o->ke32[q];
+            long long up32 = (long long)o->npairs[a] * ((o->npairs[b] + e.qb32 - 1) / e.qb32);
+            if (int er = launch_class(e.k32, grid_for(o, up32), e.smem32, d, c, 0, st)) return er;
+            ++launches;
+        }
+    }
+    {
+        int grid = (int)std::min<size_t>((nn * n_dm + 255) / 256, (size_t)o->sm_count * 8);
+        epilogue_kernel<<<grid, 256, 0, st>>>(o->jt, o->kt, n_dm, nao, hermi, with_j, with_k, vj, vk);
+        ++launches;
+    }
+    CK(cudaGetLastError());
+    if (want_stats) {
+        std::memset(stats, 0, sizeof(*stats));
+        std::vector<unsigned long long> cnt(4 * NQCLASS);
+        CK(cudaStreamSynchronize(st));
+        CK(cudaMemcpy(cnt.data(), o->counters, sizeof(unsigned long long) * cnt.size(), cudaMemcpyDeviceToHost));
+        for (int q = 0; q < NQCLASS; ++q) {
+            const ClassEntry &e = g_tab[q];
+            for (int prec = 0; prec < 2; ++prec) {
+                int64_t nq = (int64_t)cnt[2 * (q + prec * NQCLASS)];
+                int64_t np = (int64_t)cnt[2 * (q + prec * NQCLASS) + 1];
+                int64_t fl = jk_flop_model(e.li, e.lj, e.lk, e.ll, nq, np, n_dm);
+                if (prec == 0) { stats->quartets_fp64 += nq; stats->prim_quartets_fp64 += np; stats->flops_fp64 += fl; }
+                else { stats->quartets_fp32 += nq; stats->prim_quartets_fp32 += np; stats->flops_fp32 += fl; }
+            }
+        }
+        stats->kernel_launches = launches;
+        stats->n_classes = (int)o->plan_classes.size();
+    }
+    return 0;
+}
+
+}  // extern "C"

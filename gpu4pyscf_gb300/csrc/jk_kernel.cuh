@@ -1,0 +1,415 @@
+// Per-class Rys J/K kernel template (see jk_device.cuh for the scheme).
+#pragma once
+#include "jk_device.cuh"
+#include "rys_roots.cuh"
+
+namespace jk {
+
+enum { MODE_JK = 0, MODE_DIAG = 1 };
+
+constexpr double TWO_PI25 = 34.98683665524972497;  // 2 * pi^(5/2)
+
+__device__ __forceinline__ void cart_xyz(int l, int c, int &x, int &y, int &z) {
+    int idx = 0;
+    for (int lx = l; lx >= 0; --lx)
+        for (int ly = l - lx; ly >= 0; --ly) {
+            if (idx == c) { x = lx; y = ly; z = l - lx - ly; return; }
+            ++idx;
+        }
+    x = y = z = 0;
+}
+
+struct SlotInfo {
+    int valid, ish, jsh, ksh, lsh;
+    int pb_off, npb, pk_off, npk, nsteps;
+    float fac;
+    int pair;  // bra pair index (Schwarz mode)
+};
+
+template <typename Real>
+__device__ __forceinline__ const Real *dm_ptr(const EngineDev &d, bool jpart, int idm);
+template <>
+__device__ __forceinline__ const double *dm_ptr<double>(const EngineDev &d, bool jpart, int idm) {
+    size_t nn = (size_t)d.nao * d.nao;
+    return jpart ? d.dmj + idm * nn : d.dmk + idm * nn;
+}
+template <>
+__device__ __forceinline__ const float *dm_ptr<float>(const EngineDev &d, bool jpart, int idm) {
+    size_t nn = (size_t)d.nao * d.nao;
+    return jpart ? d.dmj_f + idm * nn : d.dmk_f + idm * nn;
+}
+
+template <int LI, int LJ, int LK, int LL, typename Real, int MODE>
+__global__ void __launch_bounds__(JK_THREADS)
+rys_class_kernel(EngineDev d, ClassDev c, int ntiles_static)
+{
+    using S = ClassShape<LI, LJ, LK, LL, Real>;
+    constexpr int NR = S::NR, G = S::G, QB = S::QB, NPT = S::NPT, NF = S::NF, GS = S::GS;
+    constexpr int NFI = S::NFI, NFJ = S::NFJ, NFK = S::NFK, NFL = S::NFL;
+    constexpr int IJ = S::IJ, KL = S::KL, GSKL = S::GSKL, NSC = S::NSC;
+    constexpr int GREG = (S::g_bytes(QB) > S::e_bytes(QB) ? S::g_bytes(QB) : S::e_bytes(QB)) / (int)sizeof(Real);
+
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    Real *gbuf = reinterpret_cast<Real *>(smem_raw);          // [QB][NR][3][GS]  or E[QB][NF]
+    Real *rw = gbuf + GREG;                                     // [QB][NR][2]
+    Real *sc = rw + QB * NR * 2;                                // [QB][NSC]
+    __shared__ SlotInfo slots[QB];
+    __shared__ unsigned int smax[MODE == MODE_DIAG ? QB : 1];
+    __shared__ int wmax[JK_THREADS / 32];
+
+    const int tid = threadIdx.x;
+    const int s_own = tid / G;      // quartet slot owned in S3
+    const int gl = tid % G;
+
+    // element -> packed (ix, iy, iz) indices into the 2D integral arrays
+    int eidx[NPT];
+#pragma unroll
+    for (int k = 0; k < NPT; ++k) {
+        int e = gl + k * G;
+        if (e < NF) {
+            int dd = e % NFL, t = e / NFL;
+            int cc = t % NFK; t /= NFK;
+            int bb = t % NFJ;
+            int aa = t / NFJ;
+            int ax, ay, az, bx, by, bz, cx, cy, cz, dx, dy, dz;
+            cart_xyz(LI, aa, ax, ay, az);
+            cart_xyz(LJ, bb, bx, by, bz);
+            cart_xyz(LK, cc, cx, cy, cz);
+            cart_xyz(LL, dd, dx, dy, dz);
+            int ix = ((ax * (LJ + 1) + bx) * (LK + 1) + cx) * (LL + 1) + dx;
+            int iy = ((ay * (LJ + 1) + by) * (LK + 1) + cy) * (LL + 1) + dy;
+            int iz = ((az * (LJ + 1) + bz) * (LK + 1) + cz) * (LL + 1) + dz;
+            eidx[k] = ix | (iy << 10) | (iz << 20);
+        } else {
+            eidx[k] = -1;
+        }
+    }
+
+    int ntiles = ntiles_static;
+    if (MODE == MODE_JK) ntiles = c.tile_off[c.bra.n];
+
+    for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
+        // ---- slot setup -------------------------------------------------
+        int ib = 0, kb0 = 0;
+        if (MODE == MODE_JK) {
+            int lo = 0, hi = c.bra.n;  // largest ib with tile_off[ib] <= tile
+            while (hi - lo > 1) {
+                int mid = (lo + hi) >> 1;
+                if (c.tile_off[mid] <= tile) lo = mid; else hi = mid;
+            }
+            ib = lo;
+            kb0 = c.ket_begin[ib] + (tile - c.tile_off[ib]) * QB;
+        }
+        int nst = 0;
+        if (tid < QB) {
+            SlotInfo si;
+            si.valid = 0;
+            int bra = ib, ket = 0;
+            bool ok;
+            if (MODE == MODE_JK) {
+                ket = kb0 + tid;
+                ok = ket < c.ket_end[ib];
+            } else {
+                bra = tile * QB + tid;
+                ket = bra;
+                ok = bra < c.bra.n;
+            }
+            if (ok) {
+                int2 pij = c.bra.ij[bra];
+                int2 pkl = c.ket.ij[ket];
+                if (MODE == MODE_JK) {
+                    const float *dc = d.dm_cond;
+                    int nb = d.nbas;
+                    float dmax = fmaxf(fmaxf(dc[pij.x * nb + pij.y], dc[pkl.x * nb + pkl.y]),
+                                       fmaxf(fmaxf(dc[pij.x * nb + pkl.x], dc[pij.x * nb + pkl.y]),
+                                             fmaxf(dc[pij.y * nb + pkl.x], dc[pij.y * nb + pkl.y])));
+                    ok = c.bra.logq[bra] + c.ket.logq[ket] + dmax >= d.log_cut;
+                }
+                if (ok) {
+                    si.valid = 1;
+                    si.ish = pij.x; si.jsh = pij.y; si.ksh = pkl.x; si.lsh = pkl.y;
+                    si.pb_off = c.bra.prim_off[bra];
+                    si.npb = d.shells[pij.x].nprim * d.shells[pij.y].nprim;
+                    si.pk_off = c.ket.prim_off[ket];
+                    si.npk = d.shells[pkl.x].nprim * d.shells[pkl.y].nprim;
+                    si.nsteps = si.npb * si.npk;
+                    float fac = 1.f;
+                    if (pij.x == pij.y) fac *= .5f;
+                    if (pkl.x == pkl.y) fac *= .5f;
+                    if (c.same && bra == ket) fac *= .5f;
+                    si.fac = fac;
+                    si.pair = bra;
+                    const ShellDev &A = d.shells[pij.x], &B = d.shells[pij.y];
+                    const ShellDev &C = d.shells[pkl.x], &D = d.shells[pkl.y];
+                    Real *m = sc + tid * NSC;
+                    m[14] = (Real)(A.x - B.x); m[15] = (Real)(A.y - B.y); m[16] = (Real)(A.z - B.z);
+                    m[17] = (Real)(C.x - D.x); m[18] = (Real)(C.y - D.y); m[19] = (Real)(C.z - D.z);
+                }
+            }
+            if (!si.valid) si.nsteps = 0;
+            slots[tid] = si;
+            nst = si.nsteps;
+            if (MODE == MODE_DIAG) smax[tid] = 0u;
+            if (d.counters != nullptr && MODE == MODE_JK && si.valid) {
+                atomicAdd(d.counters + 2 * c.class_id, 1ull);
+                atomicAdd(d.counters + 2 * c.class_id + 1, (unsigned long long)si.nsteps);
+            }
+        }
+        nst = __reduce_max_sync(0xffffffffu, nst);
+        if ((tid & 31) == 0) wmax[tid >> 5] = nst;
+        __syncthreads();
+        int maxsteps = 0;
+#pragma unroll
+        for (int w = 0; w < JK_THREADS / 32; ++w) maxsteps = max(maxsteps, wmax[w]);
+        if (maxsteps == 0) { __syncthreads(); continue; }
+
+        Real acc[NPT];
+#pragma unroll
+        for (int k = 0; k < NPT; ++k) acc[k] = Real(0);
+        const SlotInfo &mine = slots[s_own];
+
+        for (int step = 0; step < maxsteps; ++step) {
+            // ---- S1: roots, weights, scalars (one thread per quartet) ----
+            for (int s = tid; s < QB; s += JK_THREADS) {
+                const SlotInfo &si = slots[s];
+                if (step >= si.nsteps) continue;
+                int pb = si.pb_off + step / si.npk;
+                int pk = si.pk_off + step % si.npk;
+                Real *myrw = rw + s * NR * 2;
+                Real *m = sc + s * NSC;
+                if constexpr (sizeof(Real) == 8) {
+                    d4 a1 = d.pp_a[pb], a2 = d.pp_a[pk];
+                    d4 b1 = d.pp_b[pb], b2 = d.pp_b[pk];
+                    double ip1 = d.pp_ip[pb], ip2 = d.pp_ip[pk];
+                    double p = a1.x, q = a2.x;
+                    double rs = rsqrt(p + q);
+                    double ipq = rs * rs;
+                    double PQx = a1.y - a2.y, PQy = a1.z - a2.z, PQz = a1.w - a2.w;
+                    double T = p * q * ipq * (PQx * PQx + PQy * PQy + PQz * PQz);
+                    double pref = TWO_PI25 * b1.w * b2.w * ip1 * ip2 * rs;
+                    double u[NR], w[NR];
+                    rys_roots<NR>(T, d.rys_coef, u, w);
+#pragma unroll
+                    for (int r = 0; r < NR; ++r) { myrw[r] = (Real)u[r]; myrw[NR + r] = (Real)(w[r] * pref); }
+                    m[0] = (Real)(0.5 * ip1); m[1] = (Real)(0.5 * ip2);
+                    m[2] = (Real)(q * ipq); m[3] = (Real)(p * ipq); m[4] = (Real)(0.5 * ipq);
+                    m[5] = (Real)b1.x; m[6] = (Real)b1.y; m[7] = (Real)b1.z;
+                    m[8] = (Real)b2.x; m[9] = (Real)b2.y; m[10] = (Real)b2.z;
+                    m[11] = (Real)PQx; m[12] = (Real)PQy; m[13] = (Real)PQz;
+                } else {
+                    float4 a1 = d.pp_af[pb], a2 = d.pp_af[pk];
+                    float4 b1 = d.pp_bf[pb], b2 = d.pp_bf[pk];
+                    float ip1 = d.pp_ipf[pb], ip2 = d.pp_ipf[pk];
+                    float p = a1.x, q = a2.x;
+                    float rs = rsqrtf(p + q);
+                    float ipq = rs * rs;
+                    float PQx = a1.y - a2.y, PQy = a1.z - a2.z, PQz = a1.w - a2.w;
+                    float T = p * q * ipq * (PQx * PQx + PQy * PQy + PQz * PQz);
+                    float pref = (float)TWO_PI25 * b1.w * b2.w * ip1 * ip2 * rs;
+                    float u[NR], w[NR];
+                    rys_roots_f<NR>(T, d.rys_coef_f, u, w);
+#pragma unroll
+                    for (int r = 0; r < NR; ++r) { myrw[r] = (Real)u[r]; myrw[NR + r] = (Real)(w[r] * pref); }
+                    m[0] = (Real)(0.5f * ip1); m[1] = (Real)(0.5f * ip2);
+                    m[2] = (Real)(q * ipq); m[3] = (Real)(p * ipq); m[4] = (Real)(0.5f * ipq);
+                    m[5] = (Real)b1.x; m[6] = (Real)b1.y; m[7] = (Real)b1.z;
+                    m[8] = (Real)b2.x; m[9] = (Real)b2.y; m[10] = (Real)b2.z;
+                    m[11] = (Real)PQx; m[12] = (Real)PQy; m[13] = (Real)PQz;
+                }
+            }
+            __syncthreads();
+            // ---- S2: 2D integrals per (quartet, root, axis) ----
+            for (int task = tid; task < QB * NR * 3; task += JK_THREADS) {
+                int s = task / (NR * 3);
+                int rem = task % (NR * 3);
+                int r = rem / 3, ax = rem % 3;
+                if (step >= slots[s].nsteps) continue;
+                const Real *m = sc + s * NSC;
+                Real u = rw[s * NR * 2 + r];
+                Real i00 = (ax == 2) ? rw[s * NR * 2 + NR + r] : Real(1);
+                Real *g = gbuf + ((s * NR + r) * 3 + ax) * GS;
+                if (IJ == 0 && KL == 0) { g[0] = i00; continue; }
+                Real b00 = u * m[4];
+                Real b10 = m[0] * (Real(1) - u * m[2]);
+                Real b01 = m[1] * (Real(1) - u * m[3]);
+                Real pq = m[11 + ax];
+                Real c00 = m[5 + ax] - m[2] * u * pq;
+                Real cp00 = m[8 + ax] + m[3] * u * pq;
+                Real ab = m[14 + ax], cd = m[17 + ax];
+                Real prev[IJ + 1], cur[IJ + 1];
+                // column 0 of the vertical recurrence
+                cur[0] = i00;
+                if (IJ > 0) cur[1] = c00 * i00;
+#pragma unroll
+                for (int n = 1; n < IJ; ++n) cur[n + 1] = c00 * cur[n] + Real(n) * b10 * cur[n - 1];
+#pragma unroll
+                for (int mcol = 0; mcol <= KL; ++mcol) {
+                    if (mcol > 0) {
+                        Real nxt[IJ + 1];
+#pragma unroll
+                        for (int n = 0; n <= IJ; ++n) {
+                            Real v = cp00 * cur[n];
+                            if (mcol > 1) v += Real(mcol - 1) * b01 * prev[n];
+                            if (n > 0) v += Real(n) * b00 * cur[n - 1];
+                            nxt[n] = v;
+                        }
+#pragma unroll
+                        for (int n = 0; n <= IJ; ++n) { prev[n] = cur[n]; cur[n] = nxt[n]; }
+                    }
+                    // bra horizontal transfer on this column
+                    Real h[LJ + 1][IJ + 1];
+#pragma unroll
+                    for (int n = 0; n <= IJ; ++n) h[0][n] = cur[n];
+#pragma unroll
+                    for (int j = 1; j <= LJ; ++j)
+#pragma unroll
+                        for (int i = 0; i <= IJ - j; ++i) h[j][i] = h[j - 1][i + 1] + ab * h[j - 1][i];
+#pragma unroll
+                    for (int i = 0; i <= LI; ++i)
+#pragma unroll
+                        for (int j = 0; j <= LJ; ++j) g[(i * (LJ + 1) + j) * (KL + 1) + mcol] = h[j][i];
+                }
+                if (KL > 0) {
+                    // ket horizontal transfer in place, highest (i,j) first
+#pragma unroll
+                    for (int ij = (LI + 1) * (LJ + 1) - 1; ij >= 0; --ij) {
+                        Real t[LL + 1][KL + 1];
+#pragma unroll
+                        for (int k = 0; k <= KL; ++k) t[0][k] = g[ij * (KL + 1) + k];
+#pragma unroll
+                        for (int l = 1; l <= LL; ++l)
+#pragma unroll
+                            for (int k = 0; k <= KL - l; ++k) t[l][k] = t[l - 1][k + 1] + cd * t[l - 1][k];
+#pragma unroll
+                        for (int k = 0; k <= LK; ++k)
+#pragma unroll
+                            for (int l = 0; l <= LL; ++l) g[ij * GSKL + k * (LL + 1) + l] = t[l][k];
+                    }
+                }
+            }
+            __syncthreads();
+            // ---- S3: accumulate the Cartesian ERIs owned by this thread ----
+            if (step < mine.nsteps) {
+                const Real *gq = gbuf + s_own * NR * 3 * GS;
+#pragma unroll
+                for (int k = 0; k < NPT; ++k) {
+                    int pk = eidx[k];
+                    if (pk < 0) continue;
+                    int ix = pk & 1023, iy = (pk >> 10) & 1023, iz = pk >> 20;
+                    Real sum = Real(0);
+#pragma unroll
+                    for (int r = 0; r < NR; ++r) {
+                        const Real *gr = gq + r * 3 * GS;
+                        sum += gr[ix] * gr[GS + iy] * gr[2 * GS + iz];
+                    }
+                    acc[k] += sum;
+                }
+            }
+        }
+        __syncthreads();
+
+        if (MODE == MODE_DIAG) {
+            // Schwarz factor: max over the diagonal elements (ab|ab)
+            if (mine.valid) {
+                float mx = 0.f;
+#pragma unroll
+                for (int k = 0; k < NPT; ++k) {
+                    int e = gl + k * G;
+                    if (e >= NF) continue;
+                    int ab = e / (NFK * NFL), cd = e % (NFK * NFL);
+                    if (ab == cd) mx = fmaxf(mx, fabsf((float)acc[k]));
+                }
+                atomicMax(&smax[s_own], __float_as_uint(mx));
+            }
+            __syncthreads();
+            if (tid < QB && slots[tid].valid) d.qout[slots[tid].pair] = sqrtf(__uint_as_float(smax[tid]));
+            __syncthreads();
+            continue;
+        }
+
+        // ---- digestion: stage ERIs, contract with the densities ----
+        Real *E = gbuf;
+        if (mine.valid) {
+#pragma unroll
+            for (int k = 0; k < NPT; ++k) {
+                int e = gl + k * G;
+                if (e < NF) E[s_own * NF + e] = acc[k];
+            }
+        }
+        __syncthreads();
+        {
+            constexpr int NJ = NFI * NFJ + NFK * NFL;
+            constexpr int NK = NFI * NFK + NFI * NFL + NFJ * NFK + NFJ * NFL;
+            const int nj = d.with_j ? d.n_dm * NJ : 0;
+            const int nk = d.with_k ? d.n_dmk * NK : 0;
+            const int per = nj + nk;
+            const int nao = d.nao;
+            for (int task = tid; task < QB * per; task += JK_THREADS) {
+                int s = task / per;
+                int t = task % per;
+                const SlotInfo &si = slots[s];
+                if (!si.valid) continue;
+                const Real *Es = E + s * NF;
+                const int ai = d.shells[si.ish].ao, aj = d.shells[si.jsh].ao;
+                const int ak = d.shells[si.ksh].ao, al = d.shells[si.lsh].ao;
+                Real sum = Real(0);
+                double *out;
+                if (t < nj) {
+                    int idm = t / NJ, o = t % NJ;
+                    const Real *D = dm_ptr<Real>(d, true, idm);
+                    if (o < NFI * NFJ) {
+                        int a = o / NFJ, b = o % NFJ;
+                        const Real *Er = Es + (a * NFJ + b) * NFK * NFL;
+#pragma unroll 4
+                        for (int cc = 0; cc < NFK; ++cc)
+                            for (int dd = 0; dd < NFL; ++dd)
+                                sum += Er[cc * NFL + dd] * D[(size_t)(ak + cc) * nao + al + dd];
+                        out = d.vj + (size_t)idm * nao * nao + (size_t)(ai + a) * nao + aj + b;
+                    } else {
+                        o -= NFI * NFJ;
+                        int cc = o / NFL, dd = o % NFL;
+                        for (int a = 0; a < NFI; ++a)
+                            for (int b = 0; b < NFJ; ++b)
+                                sum += Es[(a * NFJ + b) * NFK * NFL + cc * NFL + dd] * D[(size_t)(ai + a) * nao + aj + b];
+                        out = d.vj + (size_t)idm * nao * nao + (size_t)(ak + cc) * nao + al + dd;
+                    }
+                } else {
+                    t -= nj;
+                    int idm = t / NK, o = t % NK;
+                    const Real *D = dm_ptr<Real>(d, false, idm);
+                    double *V = d.vk + (size_t)idm * nao * nao;
+                    if (o < NFI * NFK) {            // K[i a, k c] += E[abcd] D[j b, l d]
+                        int a = o / NFK, cc = o % NFK;
+                        for (int b = 0; b < NFJ; ++b)
+                            for (int dd = 0; dd < NFL; ++dd)
+                                sum += Es[((a * NFJ + b) * NFK + cc) * NFL + dd] * D[(size_t)(aj + b) * nao + al + dd];
+                        out = V + (size_t)(ai + a) * nao + ak + cc;
+                    } else if ((o -= NFI * NFK) < NFI * NFL) {   // K[i a, l d] += E D[j b, k c]
+                        int a = o / NFL, dd = o % NFL;
+                        for (int b = 0; b < NFJ; ++b)
+                            for (int cc = 0; cc < NFK; ++cc)
+                                sum += Es[((a * NFJ + b) * NFK + cc) * NFL + dd] * D[(size_t)(aj + b) * nao + ak + cc];
+                        out = V + (size_t)(ai + a) * nao + al + dd;
+                    } else if ((o -= NFI * NFL) < NFJ * NFK) {   // K[j b, k c] += E D[i a, l d]
+                        int b = o / NFK, cc = o % NFK;
+                        for (int a = 0; a < NFI; ++a)
+                            for (int dd = 0; dd < NFL; ++dd)
+                                sum += Es[((a * NFJ + b) * NFK + cc) * NFL + dd] * D[(size_t)(ai + a) * nao + al + dd];
+                        out = V + (size_t)(aj + b) * nao + ak + cc;
+                    } else {                                     // K[j b, l d] += E D[i a, k c]
+                        o -= NFJ * NFK;
+                        int b = o / NFL, dd = o % NFL;
+                        for (int a = 0; a < NFI; ++a)
+                            for (int cc = 0; cc < NFK; ++cc)
+                                sum += Es[((a * NFJ + b) * NFK + cc) * NFL + dd] * D[(size_t)(ai + a) * nao + ak + cc];
+                        out = V + (size_t)(aj + b) * nao + al + dd;
+                    }
+                }
+                atomicAdd(out, (double)si.fac * (double)sum);
+            }
+        }
+        __syncthreads();
+    }
+}
+
+}  // namespace jk

@@ -1,0 +1,35 @@
+// Registry of the per-class kernel instantiations (host side).
+#pragma once
+#include "jk_device.cuh"
+
+namespace jk {
+
+constexpr int NPAIRCLASS = (JK_LMAX + 1) * (JK_LMAX + 2) / 2;
+constexpr int NQCLASS = NPAIRCLASS * (NPAIRCLASS + 1) / 2;
+
+__host__ __device__ constexpr int pair_class(int li, int lj) { return li * (li + 1) / 2 + lj; }
+__host__ __device__ constexpr int pc_li(int pc) { int l = 0; while ((l + 1) * (l + 2) / 2 <= pc) ++l; return l; }
+__host__ __device__ constexpr int pc_lj(int pc) { return pc - pc_li(pc) * (pc_li(pc) + 1) / 2; }
+__host__ __device__ constexpr int quartet_class(int a, int b) { return a * (a + 1) / 2 + b; }  // a >= b
+
+struct ClassEntry {
+    int li, lj, lk, ll;
+    int qb64, smem64, qb32, smem32, qbdiag, smemdiag;
+    const void *k64;     // FP64 J/K kernel
+    const void *k32;     // FP32 J/K kernel
+    const void *kdiag;   // Schwarz kernel (bra class == ket class only)
+};
+
+// Defined in the instantiation translation units, one per bra pair class.
+void register_bra_class_0(ClassEntry *tab);
+void register_bra_class_1(ClassEntry *tab);
+void register_bra_class_2(ClassEntry *tab);
+void register_bra_class_3(ClassEntry *tab);
+void register_bra_class_4(ClassEntry *tab);
+void register_bra_class_5(ClassEntry *tab);
+void register_bra_class_6(ClassEntry *tab);
+void register_bra_class_7(ClassEntry *tab);
+void register_bra_class_8(ClassEntry *tab);
+void register_bra_class_9(ClassEntry *tab);
+
+}  // namespace jk

@@ -1,0 +1,84 @@
+"""Sorted, decontracted Cartesian basis for the J/K kernels.
+
+The restatement of what gpu4pyscf's SortedGTO.from_mol prepares
+(gpu4pyscf/gto/mole.py:585-654): general contractions are split into one
+shell per contraction, shells are sorted by angular momentum (then by
+primitive count, descending) and all integrals are evaluated over raw
+Cartesian functions.  The map between the user basis (spherical or
+Cartesian, any shell order) and this basis is the matrix C with
+    D_sorted = C D_user C^T,     V_user = C^T V_sorted C,
+which plays the role of SortedGTO.apply_C_mat_CT / apply_CT_mat_C
+(gpu4pyscf/gto/mole.py:906-938).
+
+Works with any molecule object exposing the libcint arrays ``_atm``,
+``_bas``, ``_env`` and ``cart`` (this package's Mole or pyscf.gto.Mole).
+"""
+
+import numpy as np
+
+from .mole import cart2sph_coeff, common_fac_sp, ncart, nsph
+
+
+class SortedBasis:
+    def __init__(self, mol):
+        self.mol = mol
+        atm = np.asarray(mol._atm, dtype=np.int32)
+        bas = np.asarray(mol._bas, dtype=np.int32)
+        env = np.asarray(mol._env, dtype=np.float64)
+        cart = bool(getattr(mol, 'cart', False))
+        # split general contractions: one (user shell, contraction) entry each
+        entries = []
+        for ib in range(len(bas)):
+            l, nprim, nctr = int(bas[ib, 1]), int(bas[ib, 2]), int(bas[ib, 3])
+            for k in range(nctr):
+                coef = env[bas[ib, 6] + k * nprim: bas[ib, 6] + (k + 1) * nprim]
+                keep = np.nonzero(coef != 0)[0]
+                entries.append((l, -len(keep), ib, k, keep))
+        order = sorted(range(len(entries)), key=lambda t: (entries[t][0], entries[t][1], t))
+        new_env = list(env[:20])
+        atm_s = atm.copy()
+        # coordinates stay where they are in env; copy them over
+        new_env = list(env)
+        new_bas = []
+        self.shell_src = []  # (user shell, contraction) of each sorted shell
+        for t in order:
+            l, _, ib, k, keep = entries[t]
+            nprim = int(bas[ib, 2])
+            exps = env[bas[ib, 5]: bas[ib, 5] + nprim][keep]
+            coef = env[bas[ib, 6] + k * nprim: bas[ib, 6] + (k + 1) * nprim][keep]
+            pe = len(new_env)
+            new_env.extend(exps.tolist())
+            pc = len(new_env)
+            new_env.extend(coef.tolist())
+            new_bas.append([bas[ib, 0], l, len(keep), 1, 0, pe, pc, 0])
+            self.shell_src.append((ib, k))
+        self._atm = atm_s
+        self._bas = np.asarray(new_bas, dtype=np.int32).reshape(-1, 8)
+        self._env = np.asarray(new_env, dtype=np.float64)
+        ls = self._bas[:, 1]
+        self.ao_loc = np.append(0, np.cumsum((ls + 1) * (ls + 2) // 2)).astype(np.int64)
+        self.nao = int(self.ao_loc[-1])
+        self.nbas = len(self._bas)
+        self.natm = len(atm)
+        self.lmax = int(ls.max()) if len(ls) else 0
+        # user AO offsets
+        ubas = bas
+        ul = ubas[:, 1]
+        unf = (ul + 1) * (ul + 2) // 2 if cart else 2 * ul + 1
+        uloc = np.append(0, np.cumsum(unf * ubas[:, 3]))
+        self.nao_user = int(uloc[-1])
+        C = np.zeros((self.nao, self.nao_user))
+        for s, (ib, k) in enumerate(self.shell_src):
+            l = int(ul[ib])
+            if cart:
+                blk = np.eye(ncart(l)) * common_fac_sp(l)
+            else:
+                blk = cart2sph_coeff(l)
+            nc, nu = blk.shape
+            u0 = uloc[ib] + k * nu
+            C[self.ao_loc[s]:self.ao_loc[s] + nc, u0:u0 + nu] = blk
+        self.coeff = C
+        self.cart = cart
+
+    def ao_loc_nr(self):
+        return self.ao_loc

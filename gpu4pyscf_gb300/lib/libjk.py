@@ -1,0 +1,73 @@
+"""ctypes binding of libgb300jk.so (C ABI declared in include/gb300jk.h).
+
+The library is built in-tree by gpu4pyscf_gb300/csrc/build.py.  There is no
+fallback: if the library is missing or fails to load, every entry point
+raises.
+"""
+import ctypes
+import os
+import threading
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_HERE, 'libgb300jk.so')
+
+JK_PREC_FP64 = 0
+JK_PREC_MIXED = 1
+
+
+class JKStats(ctypes.Structure):
+    _fields_ = [('quartets_fp64', ctypes.c_int64),
+                ('quartets_fp32', ctypes.c_int64),
+                ('prim_quartets_fp64', ctypes.c_int64),
+                ('prim_quartets_fp32', ctypes.c_int64),
+                ('flops_fp64', ctypes.c_int64),
+                ('flops_fp32', ctypes.c_int64),
+                ('kernel_launches', ctypes.c_int32),
+                ('n_classes', ctypes.c_int32)]
+
+    def as_dict(self):
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
+_lib = None
+_lock = threading.Lock()
+
+EXPORTS = ('jk_opt_create', 'jk_opt_destroy', 'jk_opt_nao', 'jk_opt_npairs',
+           'jk_opt_get_qcond', 'jk_build', 'jk_last_error')
+
+
+def load(path=None):
+    """Load the library (building it first if it does not exist)."""
+    global _lib
+    with _lock:
+        if _lib is not None:
+            return _lib
+        path = path or LIB_PATH
+        if not os.path.exists(path):
+            from ..csrc import build as _build
+            _build.build()
+        lib = ctypes.CDLL(path)
+        vp, i32, dp = ctypes.c_void_p, ctypes.c_int, ctypes.c_double
+        lib.jk_opt_create.argtypes = [vp, i32, vp, i32, vp, i32, dp, i32, ctypes.POINTER(vp)]
+        lib.jk_opt_create.restype = i32
+        lib.jk_opt_destroy.argtypes = [vp]
+        lib.jk_opt_destroy.restype = None
+        lib.jk_opt_nao.argtypes = [vp]
+        lib.jk_opt_nao.restype = i32
+        lib.jk_opt_npairs.argtypes = [vp]
+        lib.jk_opt_npairs.restype = i32
+        lib.jk_opt_get_qcond.argtypes = [vp, vp]
+        lib.jk_opt_get_qcond.restype = i32
+        lib.jk_build.argtypes = [vp, vp, i32, i32, i32, i32, i32, i32, dp, vp, vp, vp,
+                                 ctypes.POINTER(JKStats)]
+        lib.jk_build.restype = i32
+        lib.jk_last_error.argtypes = []
+        lib.jk_last_error.restype = ctypes.c_char_p
+        _lib = lib
+        return lib
+
+
+def check(code, what):
+    if code != 0:
+        msg = load().jk_last_error().decode(errors='replace')
+        raise RuntimeError('%s failed (%d): %s' % (what, code, msg))

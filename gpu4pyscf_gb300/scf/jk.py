@@ -1,0 +1,207 @@
+"""Coulomb (J) and exchange (K) matrices on the GB300 engine.
+
+Drop-in counterpart of gpu4pyscf/scf/jk.py: ``get_jk`` (jk.py:60-151),
+``get_k`` (jk.py:153-204), ``get_j`` (jk.py:206-230) and the screening
+optimizer ``_VHFOpt`` (jk.py:407-641) keep the reference's signatures,
+argument meaning (hermi 0/1/2, with_j/with_k, per-density shapes) and error
+behaviour (RuntimeError on a failed native call).  The integrals run in the
+sm_103a kernels of libgb300jk.so; there is no CPU path.
+
+Differences from the reference, by design:
+* device arrays are torch CUDA tensors (the reference uses CuPy);
+* ``_VHFOpt.precision`` ('fp64' or 'mixed') and ``_VHFOpt.split_thresh``
+  select the mixed FP32/FP64 evaluation;
+* range-separated operators (omega != 0) are not implemented and raise.
+"""
+
+import ctypes
+
+import numpy as np
+import torch
+
+from ..gto.sorted_basis import SortedBasis
+from ..lib import libjk
+
+LMAX = 3  # highest angular momentum handled by the GPU kernels (f)
+
+
+def _as_device(dm):
+    if isinstance(dm, torch.Tensor):
+        return dm.to(device='cuda', dtype=torch.float64)
+    return torch.as_tensor(np.asarray(dm, dtype=np.float64), device='cuda')
+
+
+class _VHFOpt:
+    """Screening optimizer: sorted basis, Schwarz factors, pair lists and the
+    device workspace of the engine (gpu4pyscf/scf/jk.py:407-442)."""
+
+    def __init__(self, mol, direct_scf_tol=1e-13, tile=None):
+        self.mol = mol
+        self.direct_scf_tol = direct_scf_tol
+        self.h_shls = []
+        self.tile = tile
+        self.sorted_mol = None
+        self.precision = 'fp64'
+        self.split_thresh = 1e-6
+        self._handle = None
+        self._coeff = None
+        self.last_stats = None
+
+    def reset(self, mol):
+        self._free()
+        self.mol = mol
+        self.sorted_mol = None
+        return self
+
+    def _free(self):
+        if self._handle is not None:
+            try:
+                libjk.load().jk_opt_destroy(self._handle)
+            except Exception:
+                pass
+            self._handle = None
+
+    def __del__(self):
+        self._free()
+
+    def build(self, group_size=None, verbose=None):
+        self._free()
+        smol = self.sorted_mol = SortedBasis(self.mol)
+        if smol.lmax > LMAX:
+            raise NotImplementedError(
+                'shells with l > %d are not supported by the GB300 kernels' % LMAX)
+        lib = libjk.load()
+        atm = np.ascontiguousarray(smol._atm, dtype=np.int32)
+        bas = np.ascontiguousarray(smol._bas, dtype=np.int32)
+        env = np.ascontiguousarray(smol._env, dtype=np.float64)
+        h = ctypes.c_void_p()
+        torch.cuda.current_device()
+        err = lib.jk_opt_create(atm.ctypes.data, len(atm), bas.ctypes.data, len(bas),
+                                env.ctypes.data, len(env), float(self.direct_scf_tol), 0,
+                                ctypes.byref(h))
+        libjk.check(err, 'jk_opt_create')
+        self._handle = h
+        self._coeff = torch.as_tensor(smol.coeff, device='cuda')
+        return self
+
+    @property
+    def coeff(self):
+        return self._coeff
+
+    @property
+    def nao_sorted(self):
+        return self.sorted_mol.nao
+
+    def q_cond(self):
+        """Schwarz factors sqrt(max|(ij|ij)|) of the sorted shells [nbas, nbas]."""
+        n = self.sorted_mol.nbas
+        q = np.zeros((n, n))
+        libjk.check(libjk.load().jk_opt_get_qcond(self._handle, q.ctypes.data), 'jk_opt_get_qcond')
+        return q
+
+    @property
+    def bas_pair_cache(self):
+        """{(l_i, l_j): (pair ids i*nbas+j, Schwarz factors)} of the kept pairs."""
+        q = self.q_cond()
+        n = self.sorted_mol.nbas
+        ls = self.sorted_mol._bas[:, 1]
+        out = {}
+        i, j = np.tril_indices(n)
+        keep = q[i, j] > 0
+        for a, b in zip(i[keep], j[keep]):
+            out.setdefault((int(ls[a]), int(ls[b])), []).append((a * n + b, q[a, b]))
+        return {k: (np.array([x[0] for x in v], dtype=np.uint32), np.array([x[1] for x in v]))
+                for k, v in out.items()}
+
+    # -- basis transforms (apply_coeff_C_mat_CT / CT_mat_C of the reference)
+    def apply_coeff_C_mat_CT(self, mat):
+        if self.sorted_mol is None:
+            self.build()
+        c = self._coeff
+        return torch.matmul(torch.matmul(c, mat), c.T)
+
+    def apply_coeff_CT_mat_C(self, mat):
+        if self.sorted_mol is None:
+            self.build()
+        c = self._coeff
+        return torch.matmul(torch.matmul(c.T, mat), c)
+
+    def apply_coeff_C_mat(self, mat):
+        if self.sorted_mol is None:
+            self.build()
+        return torch.matmul(self._coeff, mat)
+
+    # -- J/K in the sorted basis --------------------------------------------
+    def _build(self, dms, hermi, with_j, with_k, stats=False):
+        if self.sorted_mol is None:
+            self.build()
+        dms = dms.contiguous()
+        assert dms.ndim == 3 and dms.shape[-1] == self.sorted_mol.nao
+        n_dm, nao = dms.shape[0], dms.shape[-1]
+        vj = torch.empty_like(dms) if with_j else None
+        vk = torch.empty_like(dms) if with_k else None
+        prec = libjk.JK_PREC_MIXED if self.precision == 'mixed' else libjk.JK_PREC_FP64
+        st = libjk.JKStats() if stats else None
+        stream = torch.cuda.current_stream().cuda_stream
+        err = libjk.load().jk_build(self._handle, dms.data_ptr(), n_dm, nao, int(hermi),
+                                    int(with_j), int(with_k), prec, float(self.split_thresh),
+                                    vj.data_ptr() if with_j else None,
+                                    vk.data_ptr() if with_k else None,
+                                    stream, ctypes.byref(st) if stats else None)
+        libjk.check(err, 'jk_build')
+        if stats:
+            self.last_stats = st.as_dict()
+        return vj, vk
+
+    def get_jk(self, dms, hermi, verbose=None, stats=False):
+        """J and K for densities in the sorted basis (jk.py:492-641)."""
+        return self._build(dms, hermi, True, True, stats)
+
+    def get_j(self, dms, verbose=None):
+        return self._build(dms, 1, True, False)[0]
+
+    def get_k(self, dms, hermi, verbose=None, omega=None, lr_factor=None, sr_factor=None):
+        if omega:
+            raise NotImplementedError('range-separated K (omega != 0) is not implemented')
+        return self._build(dms, hermi, False, True)[1]
+
+
+def _check_omega(mol, omega):
+    if omega is None:
+        omega = float(getattr(mol, 'omega', 0.) or 0.)
+    if omega != 0:
+        raise NotImplementedError('range-separated operators (omega != 0) are not implemented')
+
+
+def get_jk(mol, dm, hermi=0, vhfopt=None, with_j=True, with_k=True,
+           omega=None, lr_factor=None, sr_factor=None, verbose=None):
+    """Coulomb and exchange matrices (gpu4pyscf/scf/jk.py:60-151).
+
+    dm: (nao, nao) or (n, nao, nao), numpy or torch.  Returns (vj, vk) as
+    torch CUDA tensors with the shape of dm; None for a skipped matrix.
+    """
+    assert with_j or with_k
+    _check_omega(mol, omega)
+    if vhfopt is None:
+        vhfopt = _VHFOpt(mol).build()
+    dm = _as_device(dm)
+    shape = dm.shape
+    nao = shape[-1]
+    dms = dm.reshape(-1, nao, nao)
+    dms = vhfopt.apply_coeff_C_mat_CT(dms)
+    vj, vk = vhfopt._build(dms, hermi, with_j, with_k)
+    if with_j:
+        vj = vhfopt.apply_coeff_CT_mat_C(vj).reshape(shape)
+    if with_k:
+        vk = vhfopt.apply_coeff_CT_mat_C(vk).reshape(shape)
+    return vj, vk
+
+
+def get_k(mol, dm, hermi=0, vhfopt=None, omega=None, lr_factor=None, sr_factor=None):
+    """Exchange matrix (gpu4pyscf/scf/jk.py:153-204)."""
+    return get_jk(mol, dm, hermi, vhfopt, False, True, omega, lr_factor, sr_factor)[1]
+
+
+def get_j(mol, dm, hermi=0, vhfopt=None, verbose=None):
+    """Coulomb matrix (gpu4pyscf/scf/jk.py:206-230)."""
+    return get_jk(mol, dm, hermi, vhfopt, True, False)[0]

@@ -1,0 +1,96 @@
+/* C ABI of the GB300 direct-SCF J/K engine (libgb300jk.so).
+ *
+ * Plain pointers and sizes only.  Device pointers are caller-owned CUDA
+ * device memory of the current device; the library owns a workspace inside
+ * each optimizer (pair data, screening tables, work lists, scratch
+ * accumulators).  All entry points return 0 on success or a negative error
+ * code; jk_last_error() gives a message for the last failure on the calling
+ * thread.  Work is enqueued on the caller's stream; calls on one optimizer
+ * must not overlap.
+ *
+ * Which reference interface each entry point replaces:
+ *   jk_opt_create   gpu4pyscf/scf/jk.py:407-442 (_VHFOpt.__init__/build) and
+ *                   jk.py:984-1120 (_cache_q_cond_and_non0pairs), including
+ *                   int2e_qcond_estimator (lib/gvhf-rys/nr_sr_estimator.cu:416)
+ *   jk_build        RYS_build_jk (lib/gvhf-rys/rys_contract_jk.cu:344-350),
+ *                   RYS_build_k (rys_contract_k.cu:605-612) and the class loop
+ *                   of _VHFOpt.get_jk (jk.py:492-641), for the sorted basis
+ *   jk_opt_destroy  release of the GPU caches held by _VHFOpt (jk.py:418-421)
+ *   jk_last_error   the stderr message + int status of RYS_build_jk
+ *                   (rys_contract_jk.cu:442-452)
+ */
+#ifndef GB300JK_H
+#define GB300JK_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct jk_opt jk_opt;
+
+/* Precision modes of jk_build */
+#define JK_PREC_FP64 0   /* every quartet in FP64 */
+#define JK_PREC_MIXED 1  /* quartets whose bound < split_thresh in FP32, FP64 accumulation */
+
+/* Error codes */
+#define JK_OK 0
+#define JK_ERR_ARG -1
+#define JK_ERR_CUDA -2
+#define JK_ERR_LMAX -3
+#define JK_ERR_ALLOC -4
+#define JK_ERR_OVERFLOW -5
+
+typedef struct {
+    int64_t quartets_fp64;      /* shell quartets computed in FP64 (after screening) */
+    int64_t quartets_fp32;      /* shell quartets computed in FP32 */
+    int64_t prim_quartets_fp64; /* primitive quartets behind quartets_fp64 */
+    int64_t prim_quartets_fp32;
+    int64_t flops_fp64;         /* algorithmic FLOPs of the FP64 quartets (model in the docs) */
+    int64_t flops_fp32;
+    int32_t kernel_launches;
+    int32_t n_classes;
+} jk_stats;
+
+/* Build the screening optimizer for a basis already in sorted order
+ * (shells ordered by angular momentum, one contraction per shell,
+ * coefficients including the radial normalisation, Cartesian functions).
+ * atm[natm*6], bas[nbas*8], env[nenv] use the libcint layout.
+ * tol: direct_scf_tol (quartets with bound below it are skipped).
+ * flags: reserved, pass 0. */
+int jk_opt_create(const int32_t *atm, int natm, const int32_t *bas, int nbas,
+                  const double *env, int nenv, double tol, int flags, jk_opt **out);
+
+void jk_opt_destroy(jk_opt *opt);
+
+/* Number of Cartesian AOs of the sorted basis. */
+int jk_opt_nao(const jk_opt *opt);
+
+/* Number of significant shell pairs kept after Schwarz screening. */
+int jk_opt_npairs(const jk_opt *opt);
+
+/* Per-shell-pair Schwarz factors sqrt(max|(ij|ij)|) as computed on the GPU,
+ * written to host array q[nbas*nbas] (symmetric; 0 for pruned pairs). */
+int jk_opt_get_qcond(const jk_opt *opt, double *q);
+
+/* J/K for n_dm densities in the sorted Cartesian basis.
+ * dm: device [n_dm][nao][nao] float64, C order.
+ * hermi: 0 general, 1 symmetric, 2 antisymmetric (vj set to zero).
+ * vj, vk: device [n_dm][nao][nao] float64 outputs (either may be NULL when
+ *         with_j / with_k is 0).
+ * precision: JK_PREC_FP64 or JK_PREC_MIXED with split_thresh the bound below
+ *            which a quartet is evaluated in FP32.
+ * stream: cudaStream_t of the caller (NULL = legacy default stream).
+ * stats: optional host output. */
+int jk_build(jk_opt *opt, const double *dm, int n_dm, int nao, int hermi,
+             int with_j, int with_k, int precision, double split_thresh,
+             double *vj, double *vk, void *stream, jk_stats *stats);
+
+const char *jk_last_error(void);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* GB300JK_H */

@@ -1,0 +1,80 @@
+"""Host-side logic without a GPU: basis sorting and transforms, the C ABI
+library exports, input validation."""
+import ctypes
+import os
+import re
+
+import numpy as np
+import pytest
+
+from gpu4pyscf_gb300 import gto
+from gpu4pyscf_gb300.gto.sorted_basis import SortedBasis
+from oracle import oracle as orc
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+@pytest.mark.parametrize('l', range(6))
+def test_cart2sph_matches_oracle_fit(l):
+    assert np.allclose(gto.cart2sph_coeff(l), orc.c2s_fit(l), atol=1e-11)
+
+
+@pytest.mark.parametrize('cart', [False, True])
+def test_sorted_basis_transform(cart):
+    """J/K through the sorted Cartesian basis equal the direct user-basis J/K."""
+    mol = gto.M(atom='O 0 0 0.1174; H -0.757 0 -0.4696; H 0.757 0 -0.4696',
+                basis='syn-cc-pvdz', cart=cart)
+    sb = SortedBasis(mol)
+    assert sb.nao_user == mol.nao
+    ls = sb._bas[:, 1]
+    assert np.all(np.diff(ls) >= 0)
+    assert np.all(sb._bas[:, 3] == 1)
+    rng = np.random.default_rng(0)
+    dm = rng.random((mol.nao, mol.nao))
+    dm = dm + dm.T
+    C = sb.coeff
+    dms = C @ dm @ C.T
+
+    class Raw:
+        _atm, _bas, _env = sb._atm, sb._bas, sb._env
+    vj_s, vk_s, _ = orc.get_jk_cart(Raw, dms, hermi=1)
+    vj = C.T @ vj_s @ C
+    vk = C.T @ vk_s @ C
+    vj0, vk0 = orc.get_jk(mol, dm, hermi=1)
+    assert abs(vj - vj0).max() < 1e-10
+    assert abs(vk - vk0).max() < 1e-10
+
+
+def test_basis_parsing_forms():
+    m1 = gto.M(atom='C 0 0 0', basis=('sto-3g', [[3, [1.4, 1.]]]))
+    assert list(m1._bas[:, 1]) == [0, 0, 1, 3]
+    m2 = gto.M(atom='C 0 0 0; H 0 0 1', basis={'C': 'syn-def2-svp', 'default': 'sto-3g'})
+    assert m2.nbas == 6 + 1
+    with pytest.raises(KeyError):
+        gto.M(atom='C 0 0 0', basis='def2-tzvp')
+
+
+def test_library_exports_header_symbols():
+    from gpu4pyscf_gb300.lib import libjk
+    lib = libjk.load()
+    hdr = open(os.path.join(ROOT, 'include', 'gb300jk.h')).read()
+    names = re.findall(r'^\s*(?:const\s+)?\w+\s*\*?\s*(jk_\w+)\s*\(', hdr, re.M)
+    assert set(libjk.EXPORTS) <= set(names)
+    for n in names:
+        assert hasattr(lib, n), n
+
+
+def test_lmax_above_f_rejected():
+    from gpu4pyscf_gb300.scf import jk
+    mol = gto.M(atom='C 0 0 0; H 0 0 1', basis=('sto-3g', [[4, [1., 1.]]]))
+    with pytest.raises(NotImplementedError):
+        jk._VHFOpt(mol).build()
+
+
+def test_bad_arguments_rejected_without_gpu():
+    from gpu4pyscf_gb300.lib import libjk
+    lib = libjk.load()
+    h = ctypes.c_void_p()
+    assert lib.jk_opt_create(None, 0, None, 0, None, 0, 1e-13, 0, ctypes.byref(h)) == -1
+    assert b'invalid' in lib.jk_last_error()
+    assert lib.jk_build(None, None, 1, 1, 1, 1, 1, 0, 0., None, None, None, None) == -1
