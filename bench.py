@@ -1,0 +1,361 @@
+"""Benchmark of the direct-SCF J/K build on one GB300.
+
+Workload (default --config c30): seeded synthetic 30-atom C10N3O5H12
+molecule (self-avoiding random walk, 1.0-1.5 A bonds, >= 2.0 A non-bonded),
+synthetic same-structure def2-TZVP basis (up to f), atom-block PSD FP64
+density (the sparsity of a superposition-of-atoms guess),
+direct_scf_tol 1e-13.  One step = one J/K build for that density.
+
+Printed JSON line (one per run, rank 0):
+  value       quartets/s of the FP64 build, density and pair data resident in
+              HBM, CUDA events around each build, L2 flushed between builds;
+  e2e         the same metric through the public get_jk (numpy density in
+              pinned host memory, host->device copy, basis transforms, build,
+              device->host copy of J and K inside the timed region);
+  mixed       the mixed FP32/FP64 build at split 1e-6: quartets/s, speed-up
+              over FP64 and the error against the FP64 build;
+  roofline    the dominant class kernel: algorithmic FP64 FLOP/s against the
+              FP64 FMA peak measured here by an FMA-chain probe;
+  cpu_baseline  the C++ CPU oracle on this host's cores on a bounded sample.
+
+--impl reference runs the CPU implementation of the path (the oracle, the
+restatement of PySCF's get_jk) on all host cores for the same workload.
+"""
+import argparse
+import ctypes
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+CONFIGS = {
+    'c30': dict(formula={'C': 10, 'N': 3, 'O': 5, 'H': 12}, seed=0, basis='syn-def2-tzvp',
+                workload='synthetic C10N3O5H12 (seed 0), syn-def2-tzvp, atom-block PSD density, tol 1e-13'),
+    'c10': dict(formula={'C': 4, 'N': 1, 'O': 1, 'H': 4}, seed=0, basis='syn-def2-tzvp',
+                workload='synthetic C4NOH4 (seed 0), syn-def2-tzvp, atom-block PSD density, tol 1e-13'),
+    'h2o': dict(atom='O 0 0 0.1174; H -0.757 0 -0.4696; H 0.757 0 -0.4696', basis='syn-cc-pvdz',
+                workload='H2O, syn-cc-pvdz, atom-block PSD density, tol 1e-13'),
+}
+
+
+def make_mol(cfg):
+    from gpu4pyscf_gb300 import gto
+    from gpu4pyscf_gb300.gto import molgen
+    c = CONFIGS[cfg]
+    if 'atom' in c:
+        return gto.M(atom=c['atom'], basis=c['basis'])
+    return molgen.make_mol(c['formula'], c['seed'], c['basis'])
+
+
+def make_density(mol):
+    from gpu4pyscf_gb300.scf import guess
+    return guess.block_density(mol)
+
+
+class ClockSampler:
+    def __init__(self):
+        self.proc = None
+        self.path = os.path.join(ROOT, 'gpurun_out', 'clocks_bench.csv')
+
+    def start(self):
+        try:
+            os.makedirs(os.path.dirname(self.path), exist_ok=True)
+            self.fh = open(self.path, 'w')
+            self.proc = subprocess.Popen(
+                ['nvidia-smi', '--query-gpu=index,clocks.sm,clocks.max.sm,power.draw,'
+                 'clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,'
+                 'clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,'
+                 'clocks_event_reasons.sw_power_cap', '--format=csv,noheader,nounits', '-lms', '200'],
+                stdout=self.fh, stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+
+    def stop(self):
+        if self.proc is None:
+            return None
+        self.proc.terminate()
+        self.proc.wait()
+        self.fh.close()
+        sm, smax, reasons = [], None, set()
+        names = ['hw_slowdown', 'hw_thermal_slowdown', 'sw_thermal_slowdown', 'sw_power_cap']
+        for line in open(self.path):
+            t = [x.strip() for x in line.split(',')]
+            if len(t) < 9:
+                continue
+            try:
+                sm.append(float(t[1]))
+                smax = float(t[2])
+            except ValueError:
+                continue
+            for n, v in zip(names, t[5:9]):
+                if v.lower().startswith('active'):
+                    reasons.add(n)
+        if not sm:
+            return None
+        return {'sm_mhz': float(np.median(sm)), 'sm_max_mhz': smax, 'reasons': sorted(reasons),
+                'samples': len(sm)}
+
+
+def cpu_sample(mol, dm_user, target_s=15.):
+    """Time the C++ oracle on a bounded sample of the same J/K build."""
+    from oracle import oracle
+    from gpu4pyscf_gb300.gto.sorted_basis import SortedBasis
+    sb = SortedBasis(mol)
+
+    class Raw:
+        _atm, _bas, _env = sb._atm, sb._bas, sb._env
+    dms = sb.coeff @ dm_user @ sb.coeff.T
+    npair = sb.nbas * (sb.nbas + 1) // 2
+    cores = os.cpu_count()
+    # every stride-th bra shell pair: shrink the stride until the sample
+    # takes a quarter of the target time or more
+    stride = max(npair // 64, 1)
+    while True:
+        t0 = time.perf_counter()
+        _, _, st = oracle.get_jk_cart(Raw, dms, hermi=1, tol=1e-13, nthreads=cores, bra_stride=stride)
+        dt = time.perf_counter() - t0
+        if dt > target_s / 4 or stride == 1:
+            break
+        stride = max(1, int(stride / max(2., target_s / 4 / max(dt, 1e-3))))
+    return {'value': float(st[0]) / dt, 'unit': 'quartets/s', 'cores': cores, 'kind': 'port',
+            'sample': 'C++ McMurchie-Davidson oracle (OpenMP, %d threads), every %d-th of %d bra shell '
+                      'pairs of the same sorted basis and density: %d quartets in %.2f s'
+                      % (cores, stride, npair, st[0], dt),
+            'seconds': dt, 'quartets': int(st[0]), 'stride': stride}
+
+
+def run_reference(args):
+    rank = int(os.environ.get('RANK', '0'))
+    if rank != 0:
+        return
+    mol = make_mol(args.config)
+    dm = make_density_cpu(mol)
+    ts, qs = [], 0
+    for _ in range(args.warmup):
+        pass
+    res = None
+    for _ in range(args.steps):
+        res = cpu_sample(mol, dm, target_s=args.ref_seconds)
+        ts.append(res['seconds'])
+    val = res['value']
+    line = {'impl': 'reference', 'metric': 'jk_quartets_per_s', 'value': val, 'unit': 'quartets/s',
+            'n_gpus': args.gpus, 'steps': args.steps, 'warmup': args.warmup,
+            'ms_per_step': 1e3 * float(np.mean(ts)), 'higher_is_better': True, 'scaling': 'weak',
+            'vs_baseline': None, 'dtype': 'f64', 'data': 'synthetic',
+            'config': {'workload': CONFIGS[args.config]['workload'], 'nao_user': mol.nao},
+            'cpu_baseline': {k: res[k] for k in ('value', 'unit', 'cores', 'kind', 'sample')},
+            'e2e': {'value': val, 'unit': 'quartets/s', 'h2d_bytes_per_step': 0, 'd2h_bytes_per_step': 0}}
+    print(json.dumps(line))
+
+
+def make_density_cpu(mol):
+    return make_density(mol)
+
+
+def fma_peak(lib, fp32):
+    import torch
+    out = torch.zeros(1, dtype=torch.float64, device='cuda')
+    st = torch.cuda.current_stream().cuda_stream
+    sm = torch.cuda.get_device_properties(0).multi_processor_count
+    blocks, iters = sm * 8, 4096 if not fp32 else 65536
+    lib.jk_probe_fma(out.data_ptr(), blocks, iters, fp32, st)
+    torch.cuda.synchronize()
+    best = 0.
+    for _ in range(3):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        lib.jk_probe_fma(out.data_ptr(), blocks, iters, fp32, st)
+        e1.record()
+        torch.cuda.synchronize()
+        t = e0.elapsed_time(e1) * 1e-3
+        best = max(best, blocks * 256 * iters * 8 * 2 / t)
+    return best
+
+
+def run_gpu(args):
+    import torch
+    import torch.distributed as dist
+    from gpu4pyscf_gb300.lib import libjk
+    from gpu4pyscf_gb300.scf import jk
+
+    world = int(os.environ.get('WORLD_SIZE', '1'))
+    rank = int(os.environ.get('RANK', '0'))
+    local = int(os.environ.get('LOCAL_RANK', '0'))
+    torch.cuda.set_device(local)
+    if world > 1:
+        dist.init_process_group('nccl')
+    lib = libjk.load()
+    mol = make_mol(args.config)
+    dm = make_density(mol)
+    opt = jk._VHFOpt(mol, direct_scf_tol=1e-13).build()
+    dm_dev = torch.as_tensor(dm, device='cuda')
+    dms = opt.apply_coeff_C_mat_CT(dm_dev[None]).contiguous()
+    nao_s = dms.shape[-1]
+
+    # counts for the FLOP model and the quartet rate (outside the timed region)
+    opt._build(dms, 1, True, True, stats=True)
+    st64 = dict(opt.last_stats)
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device='cuda')
+
+    def timed(fn, steps):
+        times = []
+        for _ in range(steps):
+            flush.zero_()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record()
+            fn()
+            e1.record()
+            torch.cuda.synchronize()
+            times.append(e0.elapsed_time(e1) * 1e-3)
+        return times
+
+    build64 = lambda: opt._build(dms, 1, True, True)
+    for _ in range(args.warmup):
+        build64()
+    torch.cuda.synchronize()
+    if world > 1:
+        dist.barrier()
+    clocks = ClockSampler()
+    clocks.start()
+    t64 = timed(build64, args.steps)
+    clock_info = clocks.stop()
+    tmax = torch.tensor([sum(t64)], dtype=torch.float64, device='cuda')
+    if world > 1:
+        dist.all_reduce(tmax, op=dist.ReduceOp.MAX)
+    t_step = float(tmax.item()) / args.steps
+    value = st64['quartets_fp64'] * world / t_step
+
+    # reference results for the error of the mixed build
+    vj64, vk64 = opt._build(dms, 1, True, True)
+
+    # mixed precision build
+    opt.precision, opt.split_thresh = 'mixed', args.split
+    opt._build(dms, 1, True, True, stats=True)
+    stmix = dict(opt.last_stats)
+    buildmx = lambda: opt._build(dms, 1, True, True)
+    for _ in range(args.warmup):
+        buildmx()
+    tmx = timed(buildmx, args.steps)
+    vjm, vkm = opt._build(dms, 1, True, True)
+    dmc = dms[0]
+    de = float((0.5 * torch.sum(dmc * (vjm[0] - vj64[0])) - 0.25 * torch.sum(dmc * (vkm[0] - vk64[0]))).item())
+    mixed = {'split': args.split, 'value': (stmix['quartets_fp64'] + stmix['quartets_fp32']) / (sum(tmx) / args.steps),
+             'unit': 'quartets/s', 's_per_jk_build': sum(tmx) / args.steps,
+             'speedup_vs_fp64': (sum(t64) / args.steps) / (sum(tmx) / args.steps),
+             'quartets_fp32': stmix['quartets_fp32'], 'quartets_fp64': stmix['quartets_fp64'],
+             'max_abs_dJ_sorted': float(abs(vjm - vj64).max().item()),
+             'max_abs_dK_sorted': float(abs(vkm - vk64).max().item()),
+             'dE_2e_Ha': de}
+    opt.precision = 'fp64'
+
+    # per-class kernel times (CUDA events on the build stream) for the roofline
+    h = opt._handle
+    lib.jk_opt_time_classes(h, 1)
+    opt._build(dms, 1, True, True, stats=True)
+    torch.cuda.synchronize()
+    nq = lib.jk_n_quartet_classes()
+    ms = np.zeros(2 * nq)
+    fl = np.zeros(2 * nq, dtype=np.int64)
+    qq = np.zeros(2 * nq, dtype=np.int64)
+    L = [np.zeros(nq, dtype=np.int32) for _ in range(4)]
+    best_ms = np.full(2 * nq, np.inf)
+    for _ in range(3):
+        flush.zero_()
+        opt._build(dms, 1, True, True)
+        lib.jk_opt_class_times(h, ms.ctypes.data, fl.ctypes.data, qq.ctypes.data,
+                               *[x.ctypes.data for x in L])
+        best_ms = np.minimum(best_ms, np.where(ms > 0, ms, np.inf))
+    lib.jk_opt_time_classes(h, 0)
+    best_ms[~np.isfinite(best_ms)] = 0.
+    k = int(np.argmax(best_ms[0::2])) * 2
+    peak64 = fma_peak(lib, 0)
+    peak32 = fma_peak(lib, 1)
+    dom = {'class': '(%d%d|%d%d)' % (L[0][k // 2], L[1][k // 2], L[2][k // 2], L[3][k // 2]),
+           'ms': float(best_ms[k]), 'flops': int(fl[k]), 'quartets': int(qq[k]),
+           'share_of_build': float(best_ms[k] / max(best_ms[0::2].sum(), 1e-12))}
+    achieved = fl[k] / (best_ms[k] * 1e-3) / 1e12 if best_ms[k] > 0 else 0.
+    total_fp64_tflops = st64['flops_fp64'] / t_step / 1e12
+    roofline = {'bound': 'fp64', 'achieved': achieved, 'peak': peak64 / 1e12, 'unit': 'TFLOP/s',
+                'frac': achieved / (peak64 / 1e12), 'traffic': None,
+                'kernel': 'rys_class_kernel %s FP64' % dom['class'], 'dominant': dom,
+                'peak_source': 'FP64 FMA-chain probe measured in this run (MEASURED_PEAKS.json has no FP64 figure)',
+                'fp32_peak_tflops': peak32 / 1e12,
+                'whole_build_fp64_tflops': total_fp64_tflops,
+                'whole_build_frac': total_fp64_tflops / (peak64 / 1e12)}
+    per_class = []
+    for q in range(nq):
+        if best_ms[2 * q] > 0:
+            per_class.append(['(%d%d|%d%d)' % (L[0][q], L[1][q], L[2][q], L[3][q]),
+                              round(float(best_ms[2 * q]), 4), int(qq[2 * q]), int(fl[2 * q])])
+    per_class.sort(key=lambda r: -r[1])
+
+    # end to end through the public API
+    dm_host = torch.from_numpy(np.ascontiguousarray(dm)).pin_memory()
+    out_j = torch.empty_like(dm_host).pin_memory()
+    out_k = torch.empty_like(dm_host).pin_memory()
+
+    def e2e():
+        d = dm_host.to('cuda', non_blocking=True)
+        vj, vk = jk.get_jk(mol, d, hermi=1, vhfopt=opt)
+        out_j.copy_(vj, non_blocking=True)
+        out_k.copy_(vk, non_blocking=True)
+
+    for _ in range(args.warmup):
+        e2e()
+    te = timed(e2e, args.steps)
+    e2e_val = st64['quartets_fp64'] * world / (sum(te) / args.steps)
+    nbytes = dm_host.numel() * 8
+
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu:
+        cpu = cpu_sample(mol, dm, target_s=args.cpu_seconds)
+        cpu = {k: cpu[k] for k in ('value', 'unit', 'cores', 'kind', 'sample')}
+
+    if rank == 0:
+        line = {'metric': 'jk_quartets_per_s', 'value': value, 'unit': 'quartets/s', 'n_gpus': world,
+                'steps': args.steps, 'warmup': args.warmup, 'ms_per_step': 1e3 * t_step,
+                'higher_is_better': True, 'scaling': 'weak', 'vs_baseline': None, 'dtype': 'f64',
+                'data': 'synthetic',
+                'config': {'workload': CONFIGS[args.config]['workload'], 'nao_user': mol.nao,
+                           'nao_sorted_cart': nao_s, 'n_dm': 1, 'l2': 'flushed (256 MiB write) between steps',
+                           'parallelism': 'replicas' if world > 1 else 'single GPU'},
+                's_per_jk_build': t_step, 'quartets_per_build': st64['quartets_fp64'],
+                'prim_quartets_per_build': st64['prim_quartets_fp64'],
+                'fp64_tflops_model': total_fp64_tflops,
+                'e2e': {'value': e2e_val, 'unit': 'quartets/s', 'h2d_bytes_per_step': nbytes,
+                        'd2h_bytes_per_step': 2 * nbytes, 's_per_step': sum(te) / args.steps},
+                'gpu_launches': int(st64['kernel_launches']) * args.steps,
+                'mixed': mixed, 'roofline': roofline, 'classes_top': per_class[:8],
+                'cpu_baseline': cpu, 'clocks': clock_info}
+        print(json.dumps(line))
+    if world > 1:
+        dist.destroy_process_group()
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument('--gpus', type=int, default=1)
+    ap.add_argument('--steps', type=int, default=5)
+    ap.add_argument('--warmup', type=int, default=3)
+    ap.add_argument('--impl', default='gb300', choices=['gb300', 'reference'])
+    ap.add_argument('--config', default='c30', choices=sorted(CONFIGS))
+    ap.add_argument('--split', type=float, default=1e-6)
+    ap.add_argument('--cpu-seconds', type=float, default=15.)
+    ap.add_argument('--ref-seconds', type=float, default=20.)
+    ap.add_argument('--no-cpu', action='store_true')
+    args = ap.parse_args()
+    if args.impl == 'reference':
+        run_reference(args)
+    else:
+        run_gpu(args)
+
+
+if __name__ == '__main__':
+    main()

@@ -272,6 +272,11 @@ struct jk_opt {
     float *dmj_f = nullptr, *dmk_f = nullptr;
     unsigned long long *counters = nullptr;
     std::vector<void *> owned;
+    // per-class timing (diagnostics)
+    bool time_classes = false;
+    std::vector<cudaEvent_t> ev;        // pairs of events
+    std::vector<int> ev_slot;           // 2*q + precision of each pair
+    std::vector<int64_t> last_flops, last_quartets;  // [2*NQCLASS]
 };
 
 namespace {
@@ -279,6 +284,31 @@ namespace {
 void free_all(jk_opt *o) {
     for (void *p : o->owned) cudaFree(p);
     o->owned.clear();
+    for (cudaEvent_t e : o->ev) cudaEventDestroy(e);
+    o->ev.clear();
+}
+
+__global__ void probe_fma_kernel(double *out, int iters, int fp32) {
+    double a[8];
+    float af[8];
+    for (int k = 0; k < 8; ++k) { a[k] = 1.0 + 1e-3 * (threadIdx.x + k); af[k] = (float)a[k]; }
+    const double m = 0.999999, c = 1e-7;
+    const float mf = 0.999999f, cf = 1e-7f;
+    if (fp32) {
+        for (int i = 0; i < iters; ++i)
+#pragma unroll
+            for (int k = 0; k < 8; ++k) af[k] = fmaf(af[k], mf, cf);
+        float s = 0.f;
+        for (int k = 0; k < 8; ++k) s += af[k];
+        if (s == 12345.f) out[0] = s;
+    } else {
+        for (int i = 0; i < iters; ++i)
+#pragma unroll
+            for (int k = 0; k < 8; ++k) a[k] = fma(a[k], m, c);
+        double s = 0.;
+        for (int k = 0; k < 8; ++k) s += a[k];
+        if (s == 12345.) out[0] = s;
+    }
 }
 
 template <typename T>
@@ -366,6 +396,45 @@ static int64_t jk_flop_model(int li, int lj, int lk, int ll, int64_t nquart, int
 extern "C" {
 
 const char *jk_last_error(void) { return g_last_error.c_str(); }
+
+int jk_n_quartet_classes(void) { return NQCLASS; }
+
+int jk_opt_time_classes(jk_opt *opt, int enable) {
+    if (!opt) return fail(JK_ERR_ARG, "null optimizer");
+    opt->time_classes = enable != 0;
+    return 0;
+}
+
+int jk_opt_class_times(jk_opt *opt, double *ms, int64_t *flops, int64_t *quartets,
+                       int32_t *li, int32_t *lj, int32_t *lk, int32_t *ll) {
+    if (!opt || !ms) return fail(JK_ERR_ARG, "null argument");
+    std::call_once(g_tab_once, init_registry);
+    for (int k = 0; k < 2 * NQCLASS; ++k) {
+        ms[k] = 0.;
+        if (flops) flops[k] = opt->last_flops.empty() ? 0 : opt->last_flops[k];
+        if (quartets) quartets[k] = opt->last_quartets.empty() ? 0 : opt->last_quartets[k];
+    }
+    for (size_t k = 0; k < opt->ev_slot.size(); ++k) {
+        float t = 0.f;
+        CK(cudaEventSynchronize(opt->ev[2 * k + 1]));
+        CK(cudaEventElapsedTime(&t, opt->ev[2 * k], opt->ev[2 * k + 1]));
+        ms[opt->ev_slot[k]] += t;
+    }
+    for (int q = 0; q < NQCLASS; ++q) {
+        if (li) li[q] = g_tab[q].li;
+        if (lj) lj[q] = g_tab[q].lj;
+        if (lk) lk[q] = g_tab[q].lk;
+        if (ll) ll[q] = g_tab[q].ll;
+    }
+    return 0;
+}
+
+int jk_probe_fma(double *out, int blocks, int iters, int fp32, void *stream) {
+    if (!out || blocks <= 0 || iters <= 0) return fail(JK_ERR_ARG, "jk_probe_fma: invalid arguments");
+    probe_fma_kernel<<<blocks, 256, 0, (cudaStream_t)stream>>>(out, iters, fp32);
+    CK(cudaGetLastError());
+    return 0;
+}
 
 int jk_opt_nao(const jk_opt *opt) { return opt ? opt->nao : -1; }
 
@@ -653,7 +722,15 @@ int jk_build(jk_opt *o, const double *dm, int n_dm, int nao, int hermi, int with
     d.with_j = with_j && hermi != 2;
     d.with_k = with_k;
     d.log_cut = o->tol > 0 ? (float)std::log(o->tol) : -1e30f;
-    if (!d.with_j && !d.with_k) d.with_k = 0;
+    o->ev_slot.clear();
+    if (o->time_classes) {
+        size_t need = 4 * o->plan_classes.size();
+        while (o->ev.size() < need) {
+            cudaEvent_t e;
+            CK(cudaEventCreate(&e));
+            o->ev.push_back(e);
+        }
+    }
     for (int q : o->plan_classes) {
         const ClassEntry &e = g_tab[q];
         int a = 0;
@@ -669,13 +746,17 @@ int jk_build(jk_opt *o, const double *dm, int n_dm, int nao, int hermi, int with
         c.class_id = q;
         d.counters = want_stats ? o->counters : nullptr;
         c.tile_off = o->off64[q]; c.ket_begin = o->kb64[q]; c.ket_end = o->ke64[q];
+        if (o->time_classes) { o->ev_slot.push_back(2 * q); CK(cudaEventRecord(o->ev[2 * (o->ev_slot.size() - 1)], st)); }
         if (int er = launch_class(e.k64, grid_for(o, upper), e.smem64, d, c, 0, st)) return er;
+        if (o->time_classes) CK(cudaEventRecord(o->ev[2 * (o->ev_slot.size() - 1) + 1], st));
         ++launches;
         if (mixed) {
             c.class_id = NQCLASS + q;  // FP32 counters in the second half
             c.tile_off = o->off32[q]; c.ket_begin = o->kb32[q]; c.ket_end = o->ke32[q];
             long long up32 = (long long)o->npairs[a] * ((o->npairs[b] + e.qb32 - 1) / e.qb32);
+            if (o->time_classes) { o->ev_slot.push_back(2 * q + 1); CK(cudaEventRecord(o->ev[2 * (o->ev_slot.size() - 1)], st)); }
             if (int er = launch_class(e.k32, grid_for(o, up32), e.smem32, d, c, 0, st)) return er;
+            if (o->time_classes) CK(cudaEventRecord(o->ev[2 * (o->ev_slot.size() - 1) + 1], st));
             ++launches;
         }
     }
@@ -688,6 +769,8 @@ int jk_build(jk_opt *o, const double *dm, int n_dm, int nao, int hermi, int with
     if (want_stats) {
         std::memset(stats, 0, sizeof(*stats));
         std::vector<unsigned long long> cnt(4 * NQCLASS);
+        o->last_flops.assign(2 * NQCLASS, 0);
+        o->last_quartets.assign(2 * NQCLASS, 0);
         CK(cudaStreamSynchronize(st));
         CK(cudaMemcpy(cnt.data(), o->counters, sizeof(unsigned long long) * cnt.size(), cudaMemcpyDeviceToHost));
         for (int q = 0; q < NQCLASS; ++q) {
@@ -696,6 +779,8 @@ int jk_build(jk_opt *o, const double *dm, int n_dm, int nao, int hermi, int with
                 int64_t nq = (int64_t)cnt[2 * (q + prec * NQCLASS)];
                 int64_t np = (int64_t)cnt[2 * (q + prec * NQCLASS) + 1];
                 int64_t fl = jk_flop_model(e.li, e.lj, e.lk, e.ll, nq, np, n_dm);
+                o->last_flops[2 * q + prec] = fl;
+                o->last_quartets[2 * q + prec] = nq;
                 if (prec == 0) { stats->quartets_fp64 += nq; stats->prim_quartets_fp64 += np; stats->flops_fp64 += fl; }
                 else { stats->quartets_fp32 += nq; stats->prim_quartets_fp32 += np; stats->flops_fp32 += fl; }
             }

@@ -33,7 +33,8 @@ _lib = None
 _lock = threading.Lock()
 
 EXPORTS = ('jk_opt_create', 'jk_opt_destroy', 'jk_opt_nao', 'jk_opt_npairs',
-           'jk_opt_get_qcond', 'jk_build', 'jk_last_error')
+           'jk_opt_get_qcond', 'jk_build', 'jk_last_error', 'jk_n_quartet_classes',
+           'jk_opt_time_classes', 'jk_opt_class_times', 'jk_probe_fma')
 
 
 def load(path=None):
@@ -63,6 +64,14 @@ def load(path=None):
         lib.jk_build.restype = i32
         lib.jk_last_error.argtypes = []
         lib.jk_last_error.restype = ctypes.c_char_p
+        lib.jk_n_quartet_classes.argtypes = []
+        lib.jk_n_quartet_classes.restype = i32
+        lib.jk_opt_time_classes.argtypes = [vp, i32]
+        lib.jk_opt_time_classes.restype = i32
+        lib.jk_opt_class_times.argtypes = [vp, vp, vp, vp, vp, vp, vp, vp]
+        lib.jk_opt_class_times.restype = i32
+        lib.jk_probe_fma.argtypes = [vp, i32, i32, i32, vp]
+        lib.jk_probe_fma.restype = i32
         _lib = lib
         return lib
 

@@ -89,6 +89,24 @@ int jk_build(jk_opt *opt, const double *dm, int n_dm, int nao, int hermi,
 
 const char *jk_last_error(void);
 
+/* Diagnostics (no counterpart in the reference).
+ * jk_opt_time_classes: when enabled, every class launch of later jk_build
+ * calls is bracketed by CUDA events on the build's stream.
+ * jk_opt_class_times: after a build, per quartet class q (and precision p,
+ * index 2*q+p) the kernel time in ms and the algorithmic FLOPs counted in the
+ * last build made with stats; li/lj/lk/ll receive the angular momenta.
+ * The caller's arrays hold jk_n_quartet_classes()*2 entries (li..ll: *1). */
+int jk_n_quartet_classes(void);
+int jk_opt_time_classes(jk_opt *opt, int enable);
+int jk_opt_class_times(jk_opt *opt, double *ms, int64_t *flops, int64_t *quartets,
+                       int32_t *li, int32_t *lj, int32_t *lk, int32_t *ll);
+
+/* FMA-chain throughput probe: runs iters dependent-chain FMAs (8 chains per
+ * thread) on blocks*256 threads in FP64 (fp32=0) or FP32 (fp32=1) and writes
+ * a checksum to out[0] (device memory).  Used to measure the FP64/FP32 pipe
+ * peak that the roofline of the J/K kernels is reported against. */
+int jk_probe_fma(double *out, int blocks, int iters, int fp32, void *stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -358,11 +358,11 @@ int oracle_qcond(const int *atm, int natm, const int *bas, int nbas, const doubl
 // hermi: 0 general, 1 symmetric, 2 antisymmetric (J set to zero).
 // stats (optional, int64[4]): quartets computed, quartets screened out,
 // primitive quartets computed, shell pairs.
-// bra_limit: if >0, only quartets whose bra pair index (i*(i+1)/2+j) is below
-// it are computed (bounded CPU samples for timing).
+// bra_stride: if >1, only bra shell pairs whose index i*(i+1)/2+j is a
+// multiple of it are computed (a representative bounded sample for timing).
 int oracle_jk(const int *atm, int natm, const int *bas, int nbas, const double *env,
               const double *dm, int n_dm, int hermi, double tol, int with_j, int with_k,
-              double *vj, double *vk, int nthreads, long long bra_limit, long long *stats) {
+              double *vj, double *vk, int nthreads, long long bra_stride, long long *stats) {
     (void)natm;
     int nao;
     auto sh = make_shells(atm, bas, nbas, env, &nao);
@@ -391,7 +391,8 @@ int oracle_jk(const int *atm, int natm, const int *bas, int nbas, const double *
     std::vector<std::vector<double>> jbuf(nt), kbuf(nt);
     long long n_comp = 0, n_skip = 0, n_prim = 0;
     long long npair = (long long)nbas * (nbas + 1) / 2;
-    long long plimit = bra_limit > 0 ? std::min(bra_limit, npair) : npair;
+    long long stride = bra_stride > 1 ? bra_stride : 1;
+    long long plimit = (npair + stride - 1) / stride;
 #pragma omp parallel num_threads(nt) reduction(+:n_comp, n_skip, n_prim)
     {
         int tid = 0;
@@ -404,7 +405,8 @@ int oracle_jk(const int *atm, int natm, const int *bas, int nbas, const double *
         if (with_k) K.assign(nn * n_dm, 0.0);
         std::vector<double> blk;
 #pragma omp for schedule(dynamic)
-        for (long long ij = 0; ij < plimit; ++ij) {
+        for (long long ijs = 0; ijs < plimit; ++ijs) {
+            long long ij = ijs * stride;
             int i = (int)((std::sqrt(8.0 * ij + 1) - 1) / 2);
             while ((long long)i * (i + 1) / 2 > ij) --i;
             while ((long long)(i + 1) * (i + 2) / 2 <= ij) ++i;

@@ -167,7 +167,7 @@ def qcond(mol):
 
 
 def get_jk_cart(mol, dm_cart, hermi=1, tol=0., with_j=True, with_k=True,
-                nthreads=0, bra_limit=0):
+                nthreads=0, bra_stride=1):
     """J/K in the raw Cartesian basis; returns (vj, vk, stats)."""
     atm, bas, env = _env_args(mol)
     dms = np.ascontiguousarray(np.asarray(dm_cart, dtype=np.float64))
@@ -180,7 +180,7 @@ def get_jk_cart(mol, dm_cart, hermi=1, tol=0., with_j=True, with_k=True,
     err = lib().oracle_jk(_p(atm), len(atm), _p(bas), len(bas), _p(env), _p(dms),
                           len(dms), int(hermi), ctypes.c_double(tol), int(with_j),
                           int(with_k), _p(vj), _p(vk), int(nthreads),
-                          ctypes.c_longlong(bra_limit), _p(stats))
+                          ctypes.c_longlong(bra_stride), _p(stats))
     if err:
         raise RuntimeError('oracle_jk failed')
     return vj.reshape(shape), vk.reshape(shape), stats
