@@ -792,3 +792,149 @@ int jk_build(jk_opt *o, const double *dm, int n_dm, int nao, int hermi, int with
 }
 
 }  // extern "C"
+
+// ---------------------------------------------------------------------------
+// Allocation-free J/K build.
+//
+// Some callers cannot call cudaMalloc at the moment they need a J/K build:
+// code that runs while a CUDA stream is being captured into a graph (a
+// capture is invalidated by an allocation), a host running under a strict
+// device-memory budget that forbids growth after start-up, or a plugin
+// sandbox whose host framework owns every allocation.  jk_build grows its
+// per-call workspace on demand; jk_build_noalloc instead takes every
+// per-call buffer (density copies, J/K accumulators, screening table) from
+// the fixed device array below, which each GPU that loads this library holds
+// for the life of the process.  The optimizer itself must still be created
+// beforehand with jk_opt_create, which does allocate.
+// ---------------------------------------------------------------------------
+
+#define JK_NOALLOC_SCRATCH_BYTES (32u << 20)
+
+static __device__ __align__(256) unsigned char g_noalloc_scratch[JK_NOALLOC_SCRATCH_BYTES];
+
+namespace {
+
+constexpr int JK_NOALLOC_MAX_DEVICES = 64;
+void *g_noalloc_addr[JK_NOALLOC_MAX_DEVICES] = {nullptr};
+std::mutex g_noalloc_mu;
+
+// Device address of the scratch array for the current device.  The host
+// symbol g_noalloc_scratch is only a stand-in: its address must be resolved
+// once per device, with that device current.
+int noalloc_scratch(void **out) {
+    int dev = 0;
+    CK(cudaGetDevice(&dev));
+    if (dev < 0 || dev >= JK_NOALLOC_MAX_DEVICES) return fail(JK_ERR_ARG, "jk_build_noalloc: device index too large");
+    std::lock_guard<std::mutex> lk(g_noalloc_mu);
+    if (!g_noalloc_addr[dev]) {
+        void *p = nullptr;
+        cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+        if (e != cudaSuccess || !p)
+            return fail(JK_ERR_CUDA, std::string("jk_build_noalloc: cudaGetSymbolAddress: ") + cudaGetErrorString(e));
+        g_noalloc_addr[dev] = p;
+    }
+    *out = g_noalloc_addr[dev];
+    return 0;
+}
+
+inline size_t align256(size_t x) { return (x + 255) & ~size_t(255); }
+
+}  // namespace
+
+extern "C" int jk_noalloc_scratch_bytes(void) { return (int)JK_NOALLOC_SCRATCH_BYTES; }
+
+extern "C" int jk_build_noalloc(jk_opt *o, const double *dm, int n_dm, int nao, int hermi, int with_j, int with_k,
+                                int precision, double split_thresh, double *vj, double *vk, void *stream) {
+    if (!o || !dm || n_dm <= 0 || nao != o->nao || hermi < 0 || hermi > 2 || (!with_j && !with_k))
+        return fail(JK_ERR_ARG, "jk_build_noalloc: invalid arguments");
+    if ((with_j && !vj) || (with_k && !vk)) return fail(JK_ERR_ARG, "jk_build_noalloc: missing output buffer");
+    if (precision != JK_PREC_FP64 && precision != JK_PREC_MIXED)
+        return fail(JK_ERR_ARG, "jk_build_noalloc: bad precision");
+    if (precision == JK_PREC_MIXED && !(split_thresh > 0))
+        return fail(JK_ERR_ARG, "jk_build_noalloc: split_thresh must be > 0");
+    const int mixed = precision == JK_PREC_MIXED;
+    const size_t nn = (size_t)nao * nao;
+    const int n_dmk = hermi == 0 ? 2 * n_dm : n_dm;
+    // carve the scratch: dmj, dmk, jt, kt, [dmj_f, dmk_f], dm_cond, dm_max
+    size_t off_dmj = 0;
+    size_t off_dmk = off_dmj + align256(sizeof(double) * nn * n_dm);
+    size_t off_jt = off_dmk + align256(sizeof(double) * nn * n_dmk);
+    size_t off_kt = off_jt + align256(sizeof(double) * nn * n_dm);
+    size_t off_dmjf = off_kt + align256(sizeof(double) * nn * n_dmk);
+    size_t off_dmkf = off_dmjf + (mixed ? align256(sizeof(float) * nn * n_dm) : 0);
+    size_t off_cond = off_dmkf + (mixed ? align256(sizeof(float) * nn * n_dmk) : 0);
+    size_t off_max = off_cond + align256(sizeof(float) * (size_t)o->nbas * o->nbas);
+    size_t need = off_max + 256;
+    if (need > JK_NOALLOC_SCRATCH_BYTES) {
+        char msg[256];
+        std::snprintf(msg, sizeof(msg),
+                      "jk_build_noalloc: needs %zu bytes of scratch for nao=%d n_dm=%d, above the fixed %u bytes; "
+                      "use jk_build", need, nao, n_dm, (unsigned)JK_NOALLOC_SCRATCH_BYTES);
+        return fail(JK_ERR_OVERFLOW, msg);
+    }
+    void *base = nullptr;
+    if (int e = noalloc_scratch(&base)) return e;
+    unsigned char *b = (unsigned char *)base;
+    double *dmj = (double *)(b + off_dmj), *dmk = (double *)(b + off_dmk);
+    double *jt = (double *)(b + off_jt), *kt = (double *)(b + off_kt);
+    float *dmj_f = mixed ? (float *)(b + off_dmjf) : nullptr;
+    float *dmk_f = mixed ? (float *)(b + off_dmkf) : nullptr;
+    float *dm_cond = (float *)(b + off_cond), *dm_max = (float *)(b + off_max);
+    cudaStream_t st = (cudaStream_t)stream;
+    {
+        int grid = (int)std::min<size_t>((nn * n_dm + 255) / 256, (size_t)o->sm_count * 8);
+        prep_dm_kernel<<<grid, 256, 0, st>>>(dm, n_dm, nao, hermi, mixed, dmj, dmk, dmj_f, dmk_f);
+        int nb2 = o->nbas * o->nbas;
+        dm_cond_kernel<<<(nb2 + 255) / 256, 256, 0, st>>>(dm, n_dm, nao, o->shells, o->nbas, hermi, dm_cond);
+        max_kernel<<<1, 1024, 0, st>>>(dm_cond, nb2, dm_max);
+    }
+    if (o->nplan > 0) {
+        float log_cut = o->tol > 0 ? (float)std::log(o->tol) : -1e30f;
+        float log_split = mixed ? (float)std::log(split_thresh) : 0.f;
+        plan_kernel<<<(o->plan_total + 255) / 256, 256, 0, st>>>(o->plan_dev, o->nplan, o->plan_total, dm_max,
+                                                                 log_cut, log_split, mixed);
+        scan_kernel<<<o->nscan, 1024, 0, st>>>(o->scan_dev);
+    }
+    CK(cudaGetLastError());
+    // the accumulators keep the previous call's contents: clear them
+    CK(cudaMemsetAsync(jt, 0, sizeof(double) * nn * n_dm, st));
+    CK(cudaMemsetAsync(kt, 0, sizeof(double) * nn * n_dmk, st));
+    EngineDev d = base_engine(o);
+    d.dm_cond = dm_cond;
+    d.dmj = dmj; d.dmk = dmk; d.dmj_f = dmj_f; d.dmk_f = dmk_f;
+    d.vj = jt; d.vk = kt;
+    d.n_dm = n_dm; d.n_dmk = n_dmk;
+    d.with_j = with_j && hermi != 2;
+    d.with_k = with_k;
+    d.log_cut = o->tol > 0 ? (float)std::log(o->tol) : -1e30f;
+    d.counters = nullptr;
+    if (d.with_j || d.with_k) {
+        for (int q : o->plan_classes) {
+            const ClassEntry &e = g_tab[q];
+            int a = 0;
+            while ((a + 1) * (a + 2) / 2 <= q) ++a;
+            int bcls = q - a * (a + 1) / 2;
+            ClassDev c;
+            std::memset(&c, 0, sizeof(c));
+            c.bra = PairList{o->npairs[a], o->pl_ij[a], o->pl_logq[a], o->pl_prim[a]};
+            c.ket = PairList{o->npairs[bcls], o->pl_ij[bcls], o->pl_logq[bcls], o->pl_prim[bcls]};
+            c.same = a == bcls;
+            c.class_id = q;
+            c.tile_off = o->off64[q]; c.ket_begin = o->kb64[q]; c.ket_end = o->ke64[q];
+            long long upper = (long long)o->npairs[a] * ((o->npairs[bcls] + e.qb64 - 1) / e.qb64);
+            if (int er = launch_class(e.k64, grid_for(o, upper), e.smem64, d, c, 0, st)) return er;
+            if (mixed) {
+                c.class_id = NQCLASS + q;
+                c.tile_off = o->off32[q]; c.ket_begin = o->kb32[q]; c.ket_end = o->ke32[q];
+                long long up32 = (long long)o->npairs[a] * ((o->npairs[bcls] + e.qb32 - 1) / e.qb32);
+                if (int er = launch_class(e.k32, grid_for(o, up32), e.smem32, d, c, 0, st)) return er;
+            }
+        }
+    }
+    {
+        int grid = (int)std::min<size_t>((nn * n_dm + 255) / 256, (size_t)o->sm_count * 8);
+        epilogue_kernel<<<grid, 256, 0, st>>>(jt, kt, n_dm, nao, hermi, with_j, with_k, vj, vk);
+    }
+    CK(cudaGetLastError());
+    return 0;
+}
