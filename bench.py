@@ -2,8 +2,7 @@
 
 Workload (default --config c30): seeded synthetic 30-atom C10N3O5H12
 molecule (self-avoiding random walk, 1.0-1.5 A bonds, >= 2.0 A non-bonded),
-synthetic same-structure def2-TZVP basis (up to f), atom-block PSD FP64
-density (the sparsity of a superposition-of-atoms guess),
+synthetic same-structure def2-TZVP basis (up to f), SAD FP64 density,
 direct_scf_tol 1e-13.  One step = one J/K build for that density.
 
 Printed JSON line (one per run, rank 0):
@@ -37,11 +36,11 @@ sys.path.insert(0, ROOT)
 
 CONFIGS = {
     'c30': dict(formula={'C': 10, 'N': 3, 'O': 5, 'H': 12}, seed=0, basis='syn-def2-tzvp',
-                workload='synthetic C10N3O5H12 (seed 0), syn-def2-tzvp, atom-block PSD density, tol 1e-13'),
+                workload='synthetic C10N3O5H12 (seed 0), syn-def2-tzvp, SAD density, tol 1e-13'),
     'c10': dict(formula={'C': 4, 'N': 1, 'O': 1, 'H': 4}, seed=0, basis='syn-def2-tzvp',
-                workload='synthetic C4NOH4 (seed 0), syn-def2-tzvp, atom-block PSD density, tol 1e-13'),
+                workload='synthetic C4NOH4 (seed 0), syn-def2-tzvp, SAD density, tol 1e-13'),
     'h2o': dict(atom='O 0 0 0.1174; H -0.757 0 -0.4696; H 0.757 0 -0.4696', basis='syn-cc-pvdz',
-                workload='H2O, syn-cc-pvdz, atom-block PSD density, tol 1e-13'),
+                workload='H2O, syn-cc-pvdz, SAD density, tol 1e-13'),
 }
 
 
@@ -55,8 +54,9 @@ def make_mol(cfg):
 
 
 def make_density(mol):
+    """SAD density from the engine's own atomic SCF (GPU)."""
     from gpu4pyscf_gb300.scf import guess
-    return guess.block_density(mol)
+    return guess.sad_density(mol)
 
 
 class ClockSampler:
@@ -156,7 +156,9 @@ def run_reference(args):
 
 
 def make_density_cpu(mol):
-    return make_density(mol)
+    """SAD density from the oracle's atomic SCF (CPU only)."""
+    from oracle import oracle
+    return oracle.sad_density(mol)
 
 
 def fma_peak(lib, fp32):

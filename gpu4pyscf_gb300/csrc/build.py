@@ -23,7 +23,7 @@ FLAGS = ['-O3', '-std=c++17', '-lineinfo', '-Xcompiler', '-fPIC', '-diag-suppres
 NBRA = 10
 
 SOURCES = ['jk_device.cuh', 'jk_kernel.cuh', 'rys_roots.cuh', 'rys_tables.inc', 'jk_registry.h',
-           'jk_classes.cu', 'jk_engine.cu', 'build.py']
+           'jk_classes.cu', 'jk_engine.cu', 'int1e.cu', 'build.py']
 
 
 def _digest():
@@ -60,11 +60,12 @@ def build(force=False, verbose=False, jobs=None):
         cmds.append([NVCC] + ARCH + FLAGS + ['-DJK_BRA_CLASS=%d' % b, '-c',
                                              os.path.join(HERE, 'jk_classes.cu'), '-o', o])
         objs.append(o)
-    o = os.path.join(BUILD, 'jk_engine.o')
-    cmds.append([NVCC] + ARCH + FLAGS + ['-c', os.path.join(HERE, 'jk_engine.cu'), '-o', o])
-    objs.append(o)
+    for src in ('jk_engine.cu', 'int1e.cu'):
+        o = os.path.join(BUILD, src.replace('.cu', '.o'))
+        cmds.append([NVCC] + ARCH + FLAGS + ['-c', os.path.join(HERE, src), '-o', o])
+        objs.append(o)
     # largest classes first so the long compiles start early
-    order = list(reversed(range(len(cmds) - 1))) + [len(cmds) - 1]
+    order = list(reversed(range(NBRA))) + list(range(NBRA, len(cmds)))
     jobs = jobs or min(len(cmds), os.cpu_count() or 4)
     with concurrent.futures.ThreadPoolExecutor(jobs) as ex:
         futs = [ex.submit(_run, cmds[i]) for i in order]

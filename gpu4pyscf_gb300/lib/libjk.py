@@ -34,7 +34,8 @@ _lock = threading.Lock()
 
 EXPORTS = ('jk_opt_create', 'jk_opt_destroy', 'jk_opt_nao', 'jk_opt_npairs',
            'jk_opt_get_qcond', 'jk_build', 'jk_last_error', 'jk_n_quartet_classes',
-           'jk_opt_time_classes', 'jk_opt_class_times', 'jk_probe_fma')
+           'jk_opt_time_classes', 'jk_opt_class_times', 'jk_probe_fma', 'jk_int1e',
+           'jk_int1e_last_error')
 
 
 def load(path=None):
@@ -72,6 +73,10 @@ def load(path=None):
         lib.jk_opt_class_times.restype = i32
         lib.jk_probe_fma.argtypes = [vp, i32, i32, i32, vp]
         lib.jk_probe_fma.restype = i32
+        lib.jk_int1e.argtypes = [vp, i32, vp, i32, vp, i32, vp, vp, vp, vp]
+        lib.jk_int1e.restype = i32
+        lib.jk_int1e_last_error.argtypes = []
+        lib.jk_int1e_last_error.restype = ctypes.c_char_p
         _lib = lib
         return lib
 

@@ -1,12 +1,37 @@
 """Initial densities.
 
+sad_density: superposition of atomic densities.  Each distinct element is
+computed once in the molecule's own basis by a spin-restricted,
+spherically averaged atomic Hartree-Fock with fractional occupations of the
+ground-state configuration (e.g. O: 1s^2 2s^2 2p^4, each 2p orbital holding
+4/3 electrons), on the same GPU J/K engine; the molecular guess is the
+block-diagonal assembly of the atomic densities (the role of
+init_guess_by_minao / init_guess_by_atom in gpu4pyscf/scf/hf.py:414-561).
+
 block_density: per-atom block-diagonal positive semidefinite density (X X^T
-of seeded Gaussian X on each atom's AOs) scaled so that each block's trace
-equals the atom's electron count.  It has the atom-block sparsity of a
-superposition-of-atomic-densities guess and serves as a GPU-free density of
-realistic screening behaviour.
+of seeded Gaussian X on each atom's AOs) scaled so each block's trace is the
+atom's electron count; a GPU-free density with the block sparsity of a
+superposition-of-atoms guess.
 """
 import numpy as np
+
+# electrons per (l channel) subshell, in filling order, neutral atoms H..Ar
+_SUBSHELLS = [(0, 2), (0, 2), (1, 6), (0, 2), (1, 6)]  # 1s 2s 2p 3s 3p
+
+
+def atomic_config(z):
+    """{l: [electrons in each subshell of that l, lowest first]}."""
+    left = int(z)
+    if left > 18:
+        raise NotImplementedError('SAD configurations are tabulated for H..Ar')
+    out = {0: [], 1: []}
+    for l, cap in _SUBSHELLS:
+        if left <= 0:
+            break
+        n = min(cap, left)
+        out[l].append(n)
+        left -= n
+    return out
 
 
 def atom_ao_slices(mol):
@@ -33,4 +58,89 @@ def block_density(mol, seed=0):
         d = x @ x.T
         d *= z[ia] / np.trace(d)
         dm[lo:hi, lo:hi] = d
+    return dm
+
+
+def _ao_l(mol):
+    bas = np.asarray(mol._bas)
+    out = []
+    for ib in range(len(bas)):
+        l = int(bas[ib, 1])
+        nf = (l + 1) * (l + 2) // 2 if mol.cart else 2 * l + 1
+        out += [l] * (nf * int(bas[ib, 3]))
+    return np.array(out)
+
+
+def atom_density(symb, shells, cart=False, max_cycle=60, tol=1e-9):
+    """Spherically averaged fractional-occupation atomic density (numpy)."""
+    import torch
+    from ..gto.mole import M, charge_of
+    from . import hf, jk
+    amol = M(atom=[(symb, (0., 0., 0.))], basis={symb: shells}, unit='Bohr', cart=cart)
+    z = charge_of(symb)
+    cfg = atomic_config(z)
+    opt = jk._VHFOpt(amol).build()
+    S, T, V = hf.int1e_sorted(opt)
+    C = opt.coeff
+    S = C.T @ S @ C
+    H = C.T @ (T + V) @ C
+    s, U = torch.linalg.eigh(S)
+    keep = s > 1e-9
+    X = U[:, keep] / torch.sqrt(s[keep])
+    aol = torch.as_tensor(_ao_l(amol), device='cuda')
+    SX = S
+
+    def occupy(e, c):
+        # l character of each MO by Mulliken weights
+        w = c * (SX @ c)
+        lw = torch.stack([w[aol == l].sum(0) for l in range(int(aol.max()) + 1)])
+        lch = torch.argmax(lw, dim=0)
+        occ = torch.zeros_like(e)
+        for l, subs in cfg.items():
+            idx = torch.nonzero(lch == l).flatten()
+            idx = idx[torch.argsort(e[idx])]
+            k = 0
+            deg = 2 * l + 1
+            for n in subs:
+                occ[idx[k:k + deg]] = n / deg
+                k += deg
+        return occ
+
+    e, c = torch.linalg.eigh(X.T @ H @ X)
+    c = X @ c
+    occ = occupy(e, c)
+    dm = (c * occ) @ c.T
+    diis = hf.CDIIS(8)
+    e_last = 0.
+    for it in range(max_cycle):
+        vj, vk = jk.get_jk(amol, dm, hermi=1, vhfopt=opt)
+        f = H + vj - 0.5 * vk
+        etot = float(torch.sum(dm * (H + 0.5 * (vj - 0.5 * vk))).item())
+        err = X.T @ (f @ dm @ S - S @ dm @ f) @ X
+        fd = diis.update(f, err)
+        e, c = torch.linalg.eigh(X.T @ fd @ X)
+        c = X @ c
+        occ = occupy(e, c)
+        dm_new = (c * occ) @ c.T
+        delta = float(abs(dm_new - dm).max().item())
+        dm = dm_new
+        if abs(etot - e_last) < tol and delta < 1e-6:
+            break
+        e_last = etot
+    return dm.cpu().numpy()
+
+
+def sad_density(mol):
+    """Block-diagonal superposition of atomic densities in mol's AO basis."""
+    from ..gto.mole import std_symbol
+    n = mol.nao
+    dm = np.zeros((n, n))
+    cache = {}
+    slices = atom_ao_slices(mol)
+    for ia in range(mol.natm):
+        symb = std_symbol(mol.atom_symbol(ia))
+        if symb not in cache:
+            cache[symb] = atom_density(symb, mol._basis[symb], cart=bool(mol.cart))
+        lo, hi = slices[ia]
+        dm[lo:hi, lo:hi] = cache[symb]
     return dm

@@ -89,6 +89,16 @@ int jk_build(jk_opt *opt, const double *dm, int n_dm, int nao, int hermi,
 
 const char *jk_last_error(void);
 
+/* One-electron integrals over the raw Cartesian functions of a sorted basis
+ * (same layout rules as jk_opt_create): overlap S, kinetic T and nuclear
+ * attraction V (point nuclei of all atoms), device outputs [nao][nao].
+ * Replaces the int1e_ovlp / int1e_kin / int1e_nuc integrals that gpu4pyscf's
+ * SCF driver takes for get_ovlp / get_hcore (gpu4pyscf/scf/hf.py:138-155).
+ * Synchronises the stream before returning. */
+int jk_int1e(const int32_t *atm, int natm, const int32_t *bas, int nbas,
+             const double *env, int nenv, double *S, double *T, double *V, void *stream);
+const char *jk_int1e_last_error(void);
+
 /* Diagnostics (no counterpart in the reference).
  * jk_opt_time_classes: when enabled, every class launch of later jk_build
  * calls is bracketed by CUDA events on the build's stream.

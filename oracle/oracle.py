@@ -263,3 +263,88 @@ def rhf(mol, conv_tol=1e-10, max_cycle=100, dm0=None, tol=0.):
         e_old = e
         dm = make_dm(Fd)
     return e, dm, max_cycle
+
+
+def _ao_l(mol):
+    bas = np.asarray(mol._bas)
+    out = []
+    for ib in range(len(bas)):
+        l = int(bas[ib, 1])
+        nf = (l + 1) * (l + 2) // 2 if mol.cart else 2 * l + 1
+        out += [l] * (nf * int(bas[ib, 3]))
+    return np.array(out)
+
+
+_CFG = [(0, 2), (0, 2), (1, 6), (0, 2), (1, 6)]
+
+
+def _config(z):
+    left, out = int(z), {0: [], 1: []}
+    for l, cap in _CFG:
+        if left <= 0:
+            break
+        out[l].append(min(cap, left))
+        left -= min(cap, left)
+    return out
+
+
+def atom_density(symb, shells, cart=False, max_cycle=80, tol=1e-10):
+    """Spherically averaged fractional-occupation atomic RHF density (the
+    superposition-of-atomic-densities guess of gpu4pyscf/scf/hf.py:414-561,
+    restated in numpy on the oracle's integrals)."""
+    import scipy.linalg
+    from gpu4pyscf_gb300.gto.mole import M, charge_of
+    amol = M(atom=[(symb, (0., 0., 0.))], basis={symb: shells}, unit='Bohr', cart=cart)
+    cfg = _config(charge_of(symb))
+    S = int1e(amol, 'ovlp')
+    H = int1e(amol, 'kin') + int1e(amol, 'nuc')
+    eri_ = eri(amol)
+    aol = _ao_l(amol)
+
+    def occupy(e, c):
+        w = c * (S @ c)
+        lw = np.stack([w[aol == l].sum(0) for l in range(aol.max() + 1)])
+        lch = np.argmax(lw, axis=0)
+        occ = np.zeros_like(e)
+        for l, subs in cfg.items():
+            idx = np.nonzero(lch == l)[0]
+            idx = idx[np.argsort(e[idx])]
+            k, deg = 0, 2 * l + 1
+            for n in subs:
+                occ[idx[k:k + deg]] = n / deg
+                k += deg
+        return occ
+
+    e, c = scipy.linalg.eigh(H, S)
+    dm = (c * occupy(e, c)) @ c.T
+    e_last = 0.
+    for _ in range(max_cycle):
+        f = H + np.einsum('ijkl,ji->kl', eri_, dm) - 0.5 * np.einsum('ijkl,jk->il', eri_, dm)
+        etot = np.sum(dm * (H + f)) * .5
+        e, c = scipy.linalg.eigh(f, S)
+        new = (c * occupy(e, c)) @ c.T
+        delta = abs(new - dm).max()
+        dm = 0.5 * (dm + new) if delta > 1e-3 else new
+        if abs(etot - e_last) < tol and delta < 1e-7:
+            break
+        e_last = etot
+    return dm
+
+
+def sad_density(mol):
+    from gpu4pyscf_gb300.gto.mole import std_symbol
+    bas = np.asarray(mol._bas)
+    ls = bas[:, 1]
+    nf = (ls + 1) * (ls + 2) // 2 if mol.cart else 2 * ls + 1
+    loc = np.append(0, np.cumsum(nf * bas[:, 3]))
+    n = loc[-1]
+    dm = np.zeros((n, n))
+    cache = {}
+    for ia in range(mol.natm):
+        sh = np.nonzero(bas[:, 0] == ia)[0]
+        lo, hi = loc[sh.min()], loc[sh.max() + 1]
+        symb = std_symbol(mol.atom_symbol(ia))
+        if symb not in cache:
+            cache[symb] = atom_density(symb, mol._basis[symb], cart=bool(mol.cart))
+        dm[lo:hi, lo:hi] = cache[symb]
+    return dm

@@ -91,3 +91,16 @@ def test_jk_from_full_eri():
     vj, vk = orc.get_jk(mol, dm, hermi=0)
     assert np.allclose(vj, np.einsum('ijkl,ji->kl', eri, dm), atol=1e-11)
     assert np.allclose(vk, np.einsum('ijkl,jk->il', eri, dm), atol=1e-11)
+
+
+def test_oracle_int1e_closed_forms():
+    """Normalised spherical AOs have unit overlap; a single normalised s
+    Gaussian exp(-a r^2) on a nucleus has T = 3a/2 and V = -2 Z sqrt(2a/pi)."""
+    a = 0.83
+    mol = gto.M(atom='He 0 0 0', basis={'He': [[0, [a, 1.]]]}, unit='B')
+    assert abs(orc.int1e(mol, 'ovlp')[0, 0] - 1) < 1e-14
+    assert abs(orc.int1e(mol, 'kin')[0, 0] - 1.5 * a) < 1e-13
+    assert abs(orc.int1e(mol, 'nuc')[0, 0] + 2 * 2 * np.sqrt(2 * a / np.pi)) < 1e-13
+    mol = gto.M(atom='O 0 0 0; H 0 0.8 0.6', basis='syn-def2-tzvp')
+    s = orc.int1e(mol, 'ovlp')
+    assert abs(np.diag(s) - 1).max() < 1e-12
