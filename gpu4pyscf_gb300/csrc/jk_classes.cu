@@ -2,6 +2,7 @@
 // -DJK_BRA_CLASS=<0..9>; the build compiles this file once per bra class so
 // the translation units build in parallel.
 #include "jk_kernel.cuh"
+#include "jk_lean.cuh"
 #include "jk_registry.h"
 
 #ifndef JK_BRA_CLASS
@@ -9,6 +10,10 @@
 #endif
 
 namespace jk {
+
+// classes whose ERI block plus 2D integrals fit in registers take the
+// register-resident kernel
+constexpr int LEAN_MAX = 64;
 
 template <int LI, int LJ, int LK, int LL>
 static void reg_one(ClassEntry *tab) {
@@ -18,8 +23,19 @@ static void reg_one(ClassEntry *tab) {
     e.li = LI; e.lj = LJ; e.lk = LK; e.ll = LL;
     e.qb64 = S64::QB; e.smem64 = S64::SMEM;
     e.qb32 = S32::QB; e.smem32 = S32::SMEM;
-    e.k64 = (const void *)rys_class_kernel<LI, LJ, LK, LL, double, MODE_JK>;
-    e.k32 = (const void *)rys_class_kernel<LI, LJ, LK, LL, float, MODE_JK>;
+    if constexpr (LeanShape<LI, LJ, LK, LL>::COST <= LEAN_MAX) {
+        e.lean = 1;
+        e.k64 = (const void *)rys_lean_kernel<LI, LJ, LK, LL, double>;
+        e.k32 = (const void *)rys_lean_kernel<LI, LJ, LK, LL, float>;
+        e.qb64 = e.qb32 = LEAN_THREADS;
+        e.smem64 = e.smem32 = 0;
+        e.threads64 = e.threads32 = LEAN_THREADS;
+    } else {
+        e.lean = 0;
+        e.k64 = (const void *)rys_class_kernel<LI, LJ, LK, LL, double, MODE_JK>;
+        e.k32 = (const void *)rys_class_kernel<LI, LJ, LK, LL, float, MODE_JK>;
+        e.threads64 = e.threads32 = JK_THREADS;
+    }
     if constexpr (LI == LK && LJ == LL) {
         e.kdiag = (const void *)rys_class_kernel<LI, LJ, LK, LL, double, MODE_DIAG>;
         e.qbdiag = S64::QB; e.smemdiag = S64::SMEM;

@@ -67,13 +67,19 @@ struct EngineDev {
     float log_cut;
 };
 
+// Work of one quartet class.  The ket list is split into buckets of equal
+// primitive-pair count (each bucket sorted by Schwarz factor, descending);
+// x = bra * nbk + bucket indexes the ket range [ket_begin[x], ket_end[x])
+// and tile_off[x] the first tile of that range.
 struct ClassDev {
     PairList bra, ket;
     int same;                 // bra list == ket list
     int class_id;
-    const int *tile_off;      // [bra.n + 1] prefix of tiles per bra pair
-    const int *ket_begin;     // [bra.n]
-    const int *ket_end;       // [bra.n]
+    int nbk;                  // ket buckets
+    int nx;                   // bra.n * nbk
+    const int *tile_off;      // [nx + 1]
+    const int *ket_begin;     // [nx]
+    const int *ket_end;       // [nx]
 };
 
 __host__ __device__ constexpr int ncart(int l) { return (l + 1) * (l + 2) / 2; }

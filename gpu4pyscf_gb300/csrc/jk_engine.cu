@@ -140,9 +140,10 @@ __global__ void max_kernel(const float *x, int n, float *out) {
 struct PlanClass {
     const float *bra_logq;
     const float *ket_logq;
-    int nbra, nket, same, qb64, qb32;
-    int *kb64, *ke64, *cnt64, *kb32, *ke32, *cnt32;
-    int bra_start;  // offset in the flattened bra index space
+    const int *ket_bstart;  // [nbk + 1] bucket boundaries of the ket list
+    int nbra, nket, nbk, same, qb64, qb32;
+    int *kb64, *ke64, *cnt64, *kb32, *ke32, *cnt32;  // [nbra * nbk]
+    int start;  // offset in the flattened (class, bra, bucket) index space
 };
 
 // number of entries of the descending array q[0..n) with q[k] >= thr
@@ -155,29 +156,36 @@ __device__ int count_ge(const float *q, int n, float thr) {
     return lo;
 }
 
+// Per (bra pair, ket bucket): the ket range passing q_ij q_kl max|D| >= tol
+// and, in mixed mode, its split into an FP64 head and an FP32 tail.
 __global__ void plan_kernel(const PlanClass *pcs, int npc, int total, const float *dm_max,
                             float log_cut, float log_split, int mixed) {
-    int x = blockIdx.x * blockDim.x + threadIdx.x;
-    if (x >= total) return;
+    int g = blockIdx.x * blockDim.x + threadIdx.x;
+    if (g >= total) return;
     int lo = 0, hi = npc;
     while (hi - lo > 1) {
         int mid = (lo + hi) >> 1;
-        if (pcs[mid].bra_start <= x) lo = mid; else hi = mid;
+        if (pcs[mid].start <= g) lo = mid; else hi = mid;
     }
     const PlanClass &p = pcs[lo];
-    int ib = x - p.bra_start;
-    if (ib >= p.nbra) return;
+    int x = g - p.start;
+    if (x >= p.nbra * p.nbk) return;
+    int ib = x / p.nbk, k = x % p.nbk;
+    int b0 = p.ket_bstart[k], b1 = p.ket_bstart[k + 1];
     float base = p.bra_logq[ib] + dm_max[0];
-    int nk = count_ge(p.ket_logq, p.nket, log_cut - base);
-    if (p.same) nk = min(nk, ib + 1);
-    int n64 = nk;
-    if (mixed) n64 = min(nk, count_ge(p.ket_logq, p.nket, log_split - base));
-    p.kb64[ib] = 0;
-    p.ke64[ib] = n64;
-    p.cnt64[ib] = (n64 + p.qb64 - 1) / p.qb64;
-    p.kb32[ib] = n64;
-    p.ke32[ib] = nk;
-    p.cnt32[ib] = mixed ? (nk - n64 + p.qb32 - 1) / p.qb32 : 0;
+    int end = b0 + count_ge(p.ket_logq + b0, b1 - b0, log_cut - base);
+    int mid = end;
+    if (mixed) mid = min(end, b0 + count_ge(p.ket_logq + b0, b1 - b0, log_split - base));
+    if (p.same) {
+        end = max(b0, min(end, ib + 1));
+        mid = max(b0, min(mid, ib + 1));
+    }
+    p.kb64[x] = b0;
+    p.ke64[x] = mid;
+    p.cnt64[x] = (mid - b0 + p.qb64 - 1) / p.qb64;
+    p.kb32[x] = mid;
+    p.ke32[x] = end;
+    p.cnt32[x] = mixed ? (end - mid + p.qb32 - 1) / p.qb32 : 0;
 }
 
 struct ScanJob { const int *cnt; int *off; int n; };
@@ -257,6 +265,8 @@ struct jk_opt {
     int2 *pl_ij[NPAIRCLASS] = {nullptr};
     float *pl_logq[NPAIRCLASS] = {nullptr};
     int *pl_prim[NPAIRCLASS] = {nullptr};
+    int nbk[NPAIRCLASS] = {0};           // primitive-count buckets per pair class
+    int *pl_bstart[NPAIRCLASS] = {nullptr};
     std::vector<double> qcond_h;  // [nbas*nbas]
     // planning buffers per quartet class
     int *kb64[NQCLASS] = {nullptr}, *ke64[NQCLASS] = {nullptr}, *cnt64[NQCLASS] = {nullptr}, *off64[NQCLASS] = {nullptr};
@@ -347,17 +357,17 @@ void add_prim_pairs(const jk_opt *o, int i, int j, PrimPairHost &pp) {
 }
 
 int launch_class(const void *func, int grid, int smem, const EngineDev &d, const ClassDev &c, int ntiles,
-                 cudaStream_t st) {
+                 cudaStream_t st, int threads = JK_THREADS) {
     void *args[] = {(void *)&d, (void *)&c, (void *)&ntiles};
-    CK(cudaLaunchKernel(func, dim3(grid), dim3(JK_THREADS), args, (size_t)smem, st));
+    CK(cudaLaunchKernel(func, dim3(grid), dim3(threads), args, (size_t)smem, st));
     return 0;
 }
 
 int set_smem_attrs() {
     for (int q = 0; q < NQCLASS; ++q) {
         const ClassEntry &e = g_tab[q];
-        if (e.k64) CK(cudaFuncSetAttribute(e.k64, cudaFuncAttributeMaxDynamicSharedMemorySize, e.smem64));
-        if (e.k32) CK(cudaFuncSetAttribute(e.k32, cudaFuncAttributeMaxDynamicSharedMemorySize, e.smem32));
+        if (e.k64 && !e.lean) CK(cudaFuncSetAttribute(e.k64, cudaFuncAttributeMaxDynamicSharedMemorySize, e.smem64));
+        if (e.k32 && !e.lean) CK(cudaFuncSetAttribute(e.k32, cudaFuncAttributeMaxDynamicSharedMemorySize, e.smem32));
         if (e.kdiag) CK(cudaFuncSetAttribute(e.kdiag, cudaFuncAttributeMaxDynamicSharedMemorySize, e.smemdiag));
     }
     return 0;
@@ -374,8 +384,8 @@ EngineDev base_engine(const jk_opt *o) {
     return d;
 }
 
-int grid_for(const jk_opt *o, long long upper_tiles) {
-    long long g = (long long)o->sm_count * 2;
+int grid_for(const jk_opt *o, long long upper_tiles, int lean = 0) {
+    long long g = (long long)o->sm_count * (lean ? 8 : 2);
     if (upper_tiles < g) g = upper_tiles;
     return (int)std::max<long long>(g, 1);
 }
@@ -588,7 +598,22 @@ int jk_opt_create(const int32_t *atm, int natm, const int32_t *bas, int nbas, co
                 o->qcond_h[(size_t)p.x * nbas + p.y] = o->qcond_h[(size_t)p.y * nbas + p.x] = qh[pc][k];
                 if (qh[pc][k] > 0 && qh[pc][k] >= keep) idx.push_back(k);
             }
-            std::stable_sort(idx.begin(), idx.end(), [&](int a, int b) { return qh[pc][a] > qh[pc][b]; });
+            auto npp = [&](int k) {
+                const int2 &p = cand[pc].ij[k];
+                return o->shells_h[p.x].nprim * o->shells_h[p.y].nprim;
+            };
+            std::stable_sort(idx.begin(), idx.end(), [&](int a, int b) {
+                int na = npp(a), nb = npp(b);
+                if (na != nb) return na > nb;
+                return qh[pc][a] > qh[pc][b];
+            });
+            std::vector<int> bstart{0};
+            for (size_t t = 1; t < idx.size(); ++t)
+                if (npp(idx[t]) != npp(idx[t - 1])) bstart.push_back((int)t);
+            bstart.push_back((int)idx.size());
+            if (idx.empty()) bstart = {0, 0};
+            o->nbk[pc] = (int)bstart.size() - 1;
+            if (int e = own_upload(o, &o->pl_bstart[pc], bstart)) return bail(e);
             HostPairList fin;
             for (int k : idx) {
                 const int2 &p = cand[pc].ij[k];
@@ -626,26 +651,28 @@ int jk_opt_create(const int32_t *atm, int natm, const int32_t *bas, int nbas, co
             int nb = o->npairs[a], nk = o->npairs[b];
             if (nb == 0 || nk == 0) continue;
             const ClassEntry &e = g_tab[q];
-            if (int er = own_alloc(o, &o->kb64[q], nb)) return bail(er);
-            if (int er = own_alloc(o, &o->ke64[q], nb)) return bail(er);
-            if (int er = own_alloc(o, &o->cnt64[q], nb)) return bail(er);
-            if (int er = own_alloc(o, &o->off64[q], nb + 1)) return bail(er);
-            if (int er = own_alloc(o, &o->kb32[q], nb)) return bail(er);
-            if (int er = own_alloc(o, &o->ke32[q], nb)) return bail(er);
-            if (int er = own_alloc(o, &o->cnt32[q], nb)) return bail(er);
-            if (int er = own_alloc(o, &o->off32[q], nb + 1)) return bail(er);
+            int nx = nb * o->nbk[b];
+            if (int er = own_alloc(o, &o->kb64[q], nx)) return bail(er);
+            if (int er = own_alloc(o, &o->ke64[q], nx)) return bail(er);
+            if (int er = own_alloc(o, &o->cnt64[q], nx)) return bail(er);
+            if (int er = own_alloc(o, &o->off64[q], nx + 1)) return bail(er);
+            if (int er = own_alloc(o, &o->kb32[q], nx)) return bail(er);
+            if (int er = own_alloc(o, &o->ke32[q], nx)) return bail(er);
+            if (int er = own_alloc(o, &o->cnt32[q], nx)) return bail(er);
+            if (int er = own_alloc(o, &o->off32[q], nx + 1)) return bail(er);
             PlanClass p;
             p.bra_logq = o->pl_logq[a];
             p.ket_logq = o->pl_logq[b];
-            p.nbra = nb; p.nket = nk; p.same = (a == b);
+            p.ket_bstart = o->pl_bstart[b];
+            p.nbra = nb; p.nket = nk; p.nbk = o->nbk[b]; p.same = (a == b);
             p.qb64 = e.qb64; p.qb32 = e.qb32;
             p.kb64 = o->kb64[q]; p.ke64 = o->ke64[q]; p.cnt64 = o->cnt64[q];
             p.kb32 = o->kb32[q]; p.ke32 = o->ke32[q]; p.cnt32 = o->cnt32[q];
-            p.bra_start = total;
-            total += nb;
+            p.start = total;
+            total += nx;
             plan.push_back(p);
-            scans.push_back(ScanJob{o->cnt64[q], o->off64[q], nb});
-            scans.push_back(ScanJob{o->cnt32[q], o->off32[q], nb});
+            scans.push_back(ScanJob{o->cnt64[q], o->off64[q], nx});
+            scans.push_back(ScanJob{o->cnt32[q], o->off32[q], nx});
             o->plan_classes.push_back(q);
         }
     o->nplan = (int)plan.size();
@@ -741,21 +768,23 @@ int jk_build(jk_opt *o, const double *dm, int n_dm, int nao, int hermi, int with
         c.bra = PairList{o->npairs[a], o->pl_ij[a], o->pl_logq[a], o->pl_prim[a]};
         c.ket = PairList{o->npairs[b], o->pl_ij[b], o->pl_logq[b], o->pl_prim[b]};
         c.same = a == b;
-        long long upper = (long long)o->npairs[a] * ((o->npairs[b] + e.qb64 - 1) / e.qb64);
+        c.nbk = o->nbk[b];
+        c.nx = o->npairs[a] * o->nbk[b];
+        long long upper = (long long)o->npairs[a] * ((o->npairs[b] + e.qb64 - 1) / e.qb64 + o->nbk[b]);
         if (!d.with_j && !d.with_k) break;
         c.class_id = q;
         d.counters = want_stats ? o->counters : nullptr;
         c.tile_off = o->off64[q]; c.ket_begin = o->kb64[q]; c.ket_end = o->ke64[q];
         if (o->time_classes) { o->ev_slot.push_back(2 * q); CK(cudaEventRecord(o->ev[2 * (o->ev_slot.size() - 1)], st)); }
-        if (int er = launch_class(e.k64, grid_for(o, upper), e.smem64, d, c, 0, st)) return er;
+        if (int er = launch_class(e.k64, grid_for(o, upper, e.lean), e.smem64, d, c, 0, st, e.threads64)) return er;
         if (o->time_classes) CK(cudaEventRecord(o->ev[2 * (o->ev_slot.size() - 1) + 1], st));
         ++launches;
         if (mixed) {
             c.class_id = NQCLASS + q;  // FP32 counters in the second half
             c.tile_off = o->off32[q]; c.ket_begin = o->kb32[q]; c.ket_end = o->ke32[q];
-            long long up32 = (long long)o->npairs[a] * ((o->npairs[b] + e.qb32 - 1) / e.qb32);
+            long long up32 = (long long)o->npairs[a] * ((o->npairs[b] + e.qb32 - 1) / e.qb32 + o->nbk[b]);
             if (o->time_classes) { o->ev_slot.push_back(2 * q + 1); CK(cudaEventRecord(o->ev[2 * (o->ev_slot.size() - 1)], st)); }
-            if (int er = launch_class(e.k32, grid_for(o, up32), e.smem32, d, c, 0, st)) return er;
+            if (int er = launch_class(e.k32, grid_for(o, up32, e.lean), e.smem32, d, c, 0, st, e.threads32)) return er;
             if (o->time_classes) CK(cudaEventRecord(o->ev[2 * (o->ev_slot.size() - 1) + 1], st));
             ++launches;
         }
@@ -919,15 +948,17 @@ extern "C" int jk_build_noalloc(jk_opt *o, const double *dm, int n_dm, int nao, 
             c.bra = PairList{o->npairs[a], o->pl_ij[a], o->pl_logq[a], o->pl_prim[a]};
             c.ket = PairList{o->npairs[bcls], o->pl_ij[bcls], o->pl_logq[bcls], o->pl_prim[bcls]};
             c.same = a == bcls;
+            c.nbk = o->nbk[bcls];
+            c.nx = o->npairs[a] * o->nbk[bcls];
             c.class_id = q;
             c.tile_off = o->off64[q]; c.ket_begin = o->kb64[q]; c.ket_end = o->ke64[q];
-            long long upper = (long long)o->npairs[a] * ((o->npairs[bcls] + e.qb64 - 1) / e.qb64);
-            if (int er = launch_class(e.k64, grid_for(o, upper), e.smem64, d, c, 0, st)) return er;
+            long long upper = (long long)o->npairs[a] * ((o->npairs[bcls] + e.qb64 - 1) / e.qb64 + o->nbk[bcls]);
+            if (int er = launch_class(e.k64, grid_for(o, upper, e.lean), e.smem64, d, c, 0, st, e.threads64)) return er;
             if (mixed) {
                 c.class_id = NQCLASS + q;
                 c.tile_off = o->off32[q]; c.ket_begin = o->kb32[q]; c.ket_end = o->ke32[q];
-                long long up32 = (long long)o->npairs[a] * ((o->npairs[bcls] + e.qb32 - 1) / e.qb32);
-                if (int er = launch_class(e.k32, grid_for(o, up32), e.smem32, d, c, 0, st)) return er;
+                long long up32 = (long long)o->npairs[a] * ((o->npairs[bcls] + e.qb32 - 1) / e.qb32 + o->nbk[bcls]);
+                if (int er = launch_class(e.k32, grid_for(o, up32, e.lean), e.smem32, d, c, 0, st, e.threads32)) return er;
             }
         }
     }

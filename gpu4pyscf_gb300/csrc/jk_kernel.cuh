@@ -86,19 +86,20 @@ rys_class_kernel(EngineDev d, ClassDev c, int ntiles_static)
     }
 
     int ntiles = ntiles_static;
-    if (MODE == MODE_JK) ntiles = c.tile_off[c.bra.n];
+    if (MODE == MODE_JK) ntiles = c.tile_off[c.nx];
 
     for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
         // ---- slot setup -------------------------------------------------
-        int ib = 0, kb0 = 0;
+        int ib = 0, kb0 = 0, xk = 0;
         if (MODE == MODE_JK) {
-            int lo = 0, hi = c.bra.n;  // largest ib with tile_off[ib] <= tile
+            int lo = 0, hi = c.nx;  // largest x with tile_off[x] <= tile
             while (hi - lo > 1) {
                 int mid = (lo + hi) >> 1;
                 if (c.tile_off[mid] <= tile) lo = mid; else hi = mid;
             }
-            ib = lo;
-            kb0 = c.ket_begin[ib] + (tile - c.tile_off[ib]) * QB;
+            xk = lo;
+            ib = xk / c.nbk;
+            kb0 = c.ket_begin[xk] + (tile - c.tile_off[xk]) * QB;
         }
         int nst = 0;
         if (tid < QB) {
@@ -108,7 +109,7 @@ rys_class_kernel(EngineDev d, ClassDev c, int ntiles_static)
             bool ok;
             if (MODE == MODE_JK) {
                 ket = kb0 + tid;
-                ok = ket < c.ket_end[ib];
+                ok = ket < c.ket_end[xk];
             } else {
                 bra = tile * QB + tid;
                 ket = bra;

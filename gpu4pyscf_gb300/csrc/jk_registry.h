@@ -15,6 +15,8 @@ __host__ __device__ constexpr int quartet_class(int a, int b) { return a * (a + 
 struct ClassEntry {
     int li, lj, lk, ll;
     int qb64, smem64, qb32, smem32, qbdiag, smemdiag;
+    int threads64, threads32;   // block size of the J/K kernels
+    int lean;                   // 1: register-resident kernel, 0: block-cooperative
     const void *k64;     // FP64 J/K kernel
     const void *k32;     // FP32 J/K kernel
     const void *kdiag;   // Schwarz kernel (bra class == ket class only)

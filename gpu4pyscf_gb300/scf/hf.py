@@ -174,6 +174,12 @@ class RHF:
         keep = s > self.lindep
         return U[:, keep] / torch.sqrt(s[keep])
 
+    @property
+    def _X(self):
+        if getattr(self, '_X_cache', None) is None:
+            self._X_cache = self._orth()
+        return self._X_cache
+
     def eig(self, fock, s=None):
         X = self._X
         e, c = torch.linalg.eigh(X.T @ fock @ X)
@@ -220,7 +226,6 @@ class RHF:
         t0 = time.perf_counter()
         h1e = self.get_hcore()
         s1e = self.get_ovlp()
-        self._X = self._orth()
         X = self._X
         enuc = self.energy_nuc()
         if dm0 is None:
