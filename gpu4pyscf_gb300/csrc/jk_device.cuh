@@ -69,18 +69,32 @@ struct EngineDev {
 
 // Work of one quartet class.  The ket list is split into buckets of equal
 // primitive-pair count (each bucket sorted by Schwarz factor, descending);
-// x = bra * nbk + bucket indexes the ket range [ket_begin[x], ket_end[x])
-// and tile_off[x] the first tile of that range.
+// x = bucket * bra.n + bra indexes the ket range [ket_begin[x], ket_end[x]),
+// and the class's quartets are numbered consecutively through the x ranges:
+// quartet g lies in range x with q_off[x] <= g < q_off[x + 1], so
+// neighbouring quartets share primitive counts.
 struct ClassDev {
     PairList bra, ket;
     int same;                 // bra list == ket list
     int class_id;
     int nbk;                  // ket buckets
     int nx;                   // bra.n * nbk
-    const int *tile_off;      // [nx + 1]
+    const int *q_off;         // [nx + 1] quartet offsets
     const int *ket_begin;     // [nx]
     const int *ket_end;       // [nx]
 };
+
+// quartet g -> (range x, bra, ket)
+__device__ __forceinline__ void quartet_at(const ClassDev &c, int g, int &x, int &bra, int &ket) {
+    int lo = 0, hi = c.nx;
+    while (hi - lo > 1) {
+        int mid = (lo + hi) >> 1;
+        if (__ldg(c.q_off + mid) <= g) lo = mid; else hi = mid;
+    }
+    x = lo;
+    bra = lo % c.bra.n;
+    ket = __ldg(c.ket_begin + lo) + (g - __ldg(c.q_off + lo));
+}
 
 __host__ __device__ constexpr int ncart(int l) { return (l + 1) * (l + 2) / 2; }
 

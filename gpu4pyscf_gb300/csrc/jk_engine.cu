@@ -156,8 +156,9 @@ __device__ int count_ge(const float *q, int n, float thr) {
     return lo;
 }
 
-// Per (bra pair, ket bucket): the ket range passing q_ij q_kl max|D| >= tol
-// and, in mixed mode, its split into an FP64 head and an FP32 tail.
+// Per (ket bucket, bra pair): the ket range passing q_ij q_kl max|D| >= tol
+// and, in mixed mode, its split into an FP64 head and an FP32 tail; the
+// counts are the quartets of each range, scanned into quartet offsets.
 __global__ void plan_kernel(const PlanClass *pcs, int npc, int total, const float *dm_max,
                             float log_cut, float log_split, int mixed) {
     int g = blockIdx.x * blockDim.x + threadIdx.x;
@@ -170,7 +171,7 @@ __global__ void plan_kernel(const PlanClass *pcs, int npc, int total, const floa
     const PlanClass &p = pcs[lo];
     int x = g - p.start;
     if (x >= p.nbra * p.nbk) return;
-    int ib = x / p.nbk, k = x % p.nbk;
+    int ib = x % p.nbra, k = x / p.nbra;  // ket-bucket major
     int b0 = p.ket_bstart[k], b1 = p.ket_bstart[k + 1];
     float base = p.bra_logq[ib] + dm_max[0];
     int end = b0 + count_ge(p.ket_logq + b0, b1 - b0, log_cut - base);
@@ -182,10 +183,10 @@ __global__ void plan_kernel(const PlanClass *pcs, int npc, int total, const floa
     }
     p.kb64[x] = b0;
     p.ke64[x] = mid;
-    p.cnt64[x] = (mid - b0 + p.qb64 - 1) / p.qb64;
+    p.cnt64[x] = mid - b0;
     p.kb32[x] = mid;
     p.ke32[x] = end;
-    p.cnt32[x] = mixed ? (end - mid + p.qb32 - 1) / p.qb32 : 0;
+    p.cnt32[x] = mixed ? end - mid : 0;
 }
 
 struct ScanJob { const int *cnt; int *off; int n; };
@@ -774,14 +775,14 @@ int jk_build(jk_opt *o, const double *dm, int n_dm, int nao, int hermi, int with
         if (!d.with_j && !d.with_k) break;
         c.class_id = q;
         d.counters = want_stats ? o->counters : nullptr;
-        c.tile_off = o->off64[q]; c.ket_begin = o->kb64[q]; c.ket_end = o->ke64[q];
+        c.q_off = o->off64[q]; c.ket_begin = o->kb64[q]; c.ket_end = o->ke64[q];
         if (o->time_classes) { o->ev_slot.push_back(2 * q); CK(cudaEventRecord(o->ev[2 * (o->ev_slot.size() - 1)], st)); }
         if (int er = launch_class(e.k64, grid_for(o, upper, e.lean), e.smem64, d, c, 0, st, e.threads64)) return er;
         if (o->time_classes) CK(cudaEventRecord(o->ev[2 * (o->ev_slot.size() - 1) + 1], st));
         ++launches;
         if (mixed) {
             c.class_id = NQCLASS + q;  // FP32 counters in the second half
-            c.tile_off = o->off32[q]; c.ket_begin = o->kb32[q]; c.ket_end = o->ke32[q];
+            c.q_off = o->off32[q]; c.ket_begin = o->kb32[q]; c.ket_end = o->ke32[q];
             long long up32 = (long long)o->npairs[a] * ((o->npairs[b] + e.qb32 - 1) / e.qb32 + o->nbk[b]);
             if (o->time_classes) { o->ev_slot.push_back(2 * q + 1); CK(cudaEventRecord(o->ev[2 * (o->ev_slot.size() - 1)], st)); }
             if (int er = launch_class(e.k32, grid_for(o, up32, e.lean), e.smem32, d, c, 0, st, e.threads32)) return er;
@@ -951,12 +952,12 @@ extern "C" int jk_build_noalloc(jk_opt *o, const double *dm, int n_dm, int nao, 
             c.nbk = o->nbk[bcls];
             c.nx = o->npairs[a] * o->nbk[bcls];
             c.class_id = q;
-            c.tile_off = o->off64[q]; c.ket_begin = o->kb64[q]; c.ket_end = o->ke64[q];
+            c.q_off = o->off64[q]; c.ket_begin = o->kb64[q]; c.ket_end = o->ke64[q];
             long long upper = (long long)o->npairs[a] * ((o->npairs[bcls] + e.qb64 - 1) / e.qb64 + o->nbk[bcls]);
             if (int er = launch_class(e.k64, grid_for(o, upper, e.lean), e.smem64, d, c, 0, st, e.threads64)) return er;
             if (mixed) {
                 c.class_id = NQCLASS + q;
-                c.tile_off = o->off32[q]; c.ket_begin = o->kb32[q]; c.ket_end = o->ke32[q];
+                c.q_off = o->off32[q]; c.ket_begin = o->kb32[q]; c.ket_end = o->ke32[q];
                 long long up32 = (long long)o->npairs[a] * ((o->npairs[bcls] + e.qb32 - 1) / e.qb32 + o->nbk[bcls]);
                 if (int er = launch_class(e.k32, grid_for(o, up32, e.lean), e.smem32, d, c, 0, st, e.threads32)) return er;
             }

@@ -86,30 +86,22 @@ rys_class_kernel(EngineDev d, ClassDev c, int ntiles_static)
     }
 
     int ntiles = ntiles_static;
-    if (MODE == MODE_JK) ntiles = c.tile_off[c.nx];
+    const int total = MODE == MODE_JK ? c.q_off[c.nx] : 0;
+    if (MODE == MODE_JK) ntiles = (total + QB - 1) / QB;
 
     for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
         // ---- slot setup -------------------------------------------------
-        int ib = 0, kb0 = 0, xk = 0;
-        if (MODE == MODE_JK) {
-            int lo = 0, hi = c.nx;  // largest x with tile_off[x] <= tile
-            while (hi - lo > 1) {
-                int mid = (lo + hi) >> 1;
-                if (c.tile_off[mid] <= tile) lo = mid; else hi = mid;
-            }
-            xk = lo;
-            ib = xk / c.nbk;
-            kb0 = c.ket_begin[xk] + (tile - c.tile_off[xk]) * QB;
-        }
         int nst = 0;
         if (tid < QB) {
             SlotInfo si;
             si.valid = 0;
-            int bra = ib, ket = 0;
+            int bra = 0, ket = 0;
             bool ok;
             if (MODE == MODE_JK) {
-                ket = kb0 + tid;
-                ok = ket < c.ket_end[xk];
+                const int g = tile * QB + tid;
+                ok = g < total;
+                int xk;
+                if (ok) quartet_at(c, g, xk, bra, ket);
             } else {
                 bra = tile * QB + tid;
                 ket = bra;

@@ -1,15 +1,16 @@
 // Register-resident Rys J/K kernel for the small angular classes.
 //
 // One thread owns one shell quartet from start to end: no shared memory and
-// no barriers.  A block of LEAN_THREADS threads takes one bra pair and a run
-// of kets of one primitive-count bucket, so the threads of a warp run the
-// same number of primitive iterations.  Per primitive quartet and root the
+// no barriers.  Threads take consecutive quartets of the class's quartet
+// numbering (ket-bucket major), so the lanes of a warp are all busy and run
+// the same number of ket primitive iterations.  Per primitive quartet and root the
 // 2D integrals of the three axes live in registers (fully unrolled vertical
 // recurrence and horizontal transfers), the Cartesian ERI block accumulates
 // in registers, and after the primitive loops the thread contracts its block
 // with the six density blocks.  The J block of the bra pair, common to the
-// whole warp, is summed across the warp with shuffles before one atomic add
-// per element; the other five blocks go out with one atomic add per element.
+// warp when all its lanes share the bra pair, is summed across the warp with
+// shuffles before one atomic add per element; the other five blocks go out
+// with one atomic add per element.
 #pragma once
 #include "jk_device.cuh"
 #include "rys_roots.cuh"
@@ -107,19 +108,16 @@ rys_lean_kernel(EngineDev d, ClassDev c, int unused)
     using S = LeanShape<LI, LJ, LK, LL>;
     constexpr int NR = S::NR, NF = S::NF, GS = S::GS, GSKL = S::GSKL;
     constexpr int NFI = S::NFI, NFJ = S::NFJ, NFK = S::NFK, NFL = S::NFL;
-    const int ntiles = c.tile_off[c.nx];
+    const int total = c.q_off[c.nx];
     const int lane = threadIdx.x & 31;
-    for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
-        int lo = 0, hi = c.nx;
-        while (hi - lo > 1) {
-            int mid = (lo + hi) >> 1;
-            if (c.tile_off[mid] <= tile) lo = mid; else hi = mid;
-        }
-        const int xk = lo;
-        const int ib = xk / c.nbk;
-        const int ket = c.ket_begin[xk] + (tile - c.tile_off[xk]) * LEAN_THREADS + threadIdx.x;
+    const int stride = gridDim.x * blockDim.x;
+    // warp-uniform loop: lane 0 of every iteration holds a valid quartet
+    for (int g0 = blockIdx.x * blockDim.x + (threadIdx.x & ~31); g0 < total; g0 += stride) {
+        const int g = g0 + lane;
+        int xk, ib, ket;
+        quartet_at(c, g < total ? g : g0, xk, ib, ket);
+        bool valid = g < total;
         const int2 pij = c.bra.ij[ib];
-        bool valid = ket < c.ket_end[xk];
         int2 pkl = make_int2(0, 0);
         if (valid) {
             pkl = c.ket.ij[ket];
@@ -130,6 +128,9 @@ rys_lean_kernel(EngineDev d, ClassDev c, int unused)
                                      fmaxf(dc[pij.y * nb + pkl.x], dc[pij.y * nb + pkl.y])));
             valid = c.bra.logq[ib] + c.ket.logq[ket] + dmax >= d.log_cut;
         }
+        // the J block of the bra pair can be summed across the warp when all
+        // its lanes share the bra
+        const bool same_bra = __all_sync(0xffffffffu, ib == __shfl_sync(0xffffffffu, ib, 0));
         Real acc[NF];
 #pragma unroll
         for (int e = 0; e < NF; ++e) acc[e] = Real(0);
@@ -243,9 +244,14 @@ rys_lean_kernel(EngineDev d, ClassDev c, int unused)
 #pragma unroll
                     for (int cd = 0; cd < NFK * NFL; ++cd) s += acc[ab * NFK * NFL + cd] * dkl[cd];
                     double sd = valid ? (double)(fac * s) : 0.;
+                    double *dst = V + (size_t)(ai + ab / NFJ) * nao + aj + ab % NFJ;
+                    if (same_bra) {
 #pragma unroll
-                    for (int off = 16; off > 0; off >>= 1) sd += __shfl_xor_sync(0xffffffffu, sd, off);
-                    if (lane == 0 && sd != 0.) atomicAdd(V + (size_t)(ai + ab / NFJ) * nao + aj + ab % NFJ, sd);
+                        for (int off = 16; off > 0; off >>= 1) sd += __shfl_xor_sync(0xffffffffu, sd, off);
+                        if (lane == 0 && sd != 0.) atomicAdd(dst, sd);
+                    } else if (valid) {
+                        atomicAdd(dst, sd);
+                    }
                 }
                 if (valid) {
 #pragma unroll

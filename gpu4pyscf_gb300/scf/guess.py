@@ -72,62 +72,53 @@ def _ao_l(mol):
 
 
 def atom_density(symb, shells, cart=False, max_cycle=60, tol=1e-9):
-    """Spherically averaged fractional-occupation atomic density (numpy)."""
+    """Spherically averaged fractional-occupation atomic density (numpy).
+
+    J/K and one-electron integrals come from the GPU engine; the tiny
+    eigenproblems are solved on the host."""
+    import scipy.linalg
     import torch
     from ..gto.mole import M, charge_of
     from . import hf, jk
     amol = M(atom=[(symb, (0., 0., 0.))], basis={symb: shells}, unit='Bohr', cart=cart)
-    z = charge_of(symb)
-    cfg = atomic_config(z)
+    cfg = atomic_config(charge_of(symb))
     opt = jk._VHFOpt(amol).build()
     S, T, V = hf.int1e_sorted(opt)
     C = opt.coeff
-    S = C.T @ S @ C
-    H = C.T @ (T + V) @ C
-    s, U = torch.linalg.eigh(S)
-    keep = s > 1e-9
-    X = U[:, keep] / torch.sqrt(s[keep])
-    aol = torch.as_tensor(_ao_l(amol), device='cuda')
-    SX = S
+    S = (C.T @ S @ C).cpu().numpy()
+    H = (C.T @ (T + V) @ C).cpu().numpy()
+    aol = _ao_l(amol)
 
     def occupy(e, c):
         # l character of each MO by Mulliken weights
-        w = c * (SX @ c)
-        lw = torch.stack([w[aol == l].sum(0) for l in range(int(aol.max()) + 1)])
-        lch = torch.argmax(lw, dim=0)
-        occ = torch.zeros_like(e)
+        w = c * (S @ c)
+        lw = np.stack([w[aol == l].sum(0) for l in range(int(aol.max()) + 1)])
+        lch = np.argmax(lw, axis=0)
+        occ = np.zeros_like(e)
         for l, subs in cfg.items():
-            idx = torch.nonzero(lch == l).flatten()
-            idx = idx[torch.argsort(e[idx])]
-            k = 0
-            deg = 2 * l + 1
+            idx = np.nonzero(lch == l)[0]
+            idx = idx[np.argsort(e[idx])]
+            k, deg = 0, 2 * l + 1
             for n in subs:
                 occ[idx[k:k + deg]] = n / deg
                 k += deg
         return occ
 
-    e, c = torch.linalg.eigh(X.T @ H @ X)
-    c = X @ c
-    occ = occupy(e, c)
-    dm = (c * occ) @ c.T
-    diis = hf.CDIIS(8)
+    e, c = scipy.linalg.eigh(H, S)
+    dm = (c * occupy(e, c)) @ c.T
     e_last = 0.
     for it in range(max_cycle):
         vj, vk = jk.get_jk(amol, dm, hermi=1, vhfopt=opt)
-        f = H + vj - 0.5 * vk
-        etot = float(torch.sum(dm * (H + 0.5 * (vj - 0.5 * vk))).item())
-        err = X.T @ (f @ dm @ S - S @ dm @ f) @ X
-        fd = diis.update(f, err)
-        e, c = torch.linalg.eigh(X.T @ fd @ X)
-        c = X @ c
-        occ = occupy(e, c)
-        dm_new = (c * occ) @ c.T
-        delta = float(abs(dm_new - dm).max().item())
-        dm = dm_new
-        if abs(etot - e_last) < tol and delta < 1e-6:
+        f = H + vj.cpu().numpy() - 0.5 * vk.cpu().numpy()
+        etot = 0.5 * float(np.sum(dm * (H + f)))
+        e, c = scipy.linalg.eigh(f, S)
+        new = (c * occupy(e, c)) @ c.T
+        delta = abs(new - dm).max()
+        dm = 0.5 * (dm + new) if delta > 1e-3 else new
+        if abs(etot - e_last) < tol and delta < 1e-7:
             break
         e_last = etot
-    return dm.cpu().numpy()
+    return dm
 
 
 def sad_density(mol):
