@@ -84,6 +84,23 @@ struct ClassDev {
     const int *ket_end;       // [nx]
 };
 
+__device__ __forceinline__ void quartet_at(const ClassDev &c, int g, int &x, int &bra, int &ket);
+
+// Density screening of quartet g of the class numbering: q_ij q_kl times the
+// largest of the six density blocks it touches against the cutoff
+// (gpu4pyscf/lib/gvhf-rys/create_tasks.cu:152-162).
+__device__ __forceinline__ bool quartet_passes(const EngineDev &d, const ClassDev &c, int g) {
+    int x, bra, ket;
+    quartet_at(c, g, x, bra, ket);
+    const int2 pij = c.bra.ij[bra], pkl = c.ket.ij[ket];
+    const float *dc = d.dm_cond;
+    const int nb = d.nbas;
+    float dmax = fmaxf(fmaxf(__ldg(dc + pij.x * nb + pij.y), __ldg(dc + pkl.x * nb + pkl.y)),
+                       fmaxf(fmaxf(__ldg(dc + pij.x * nb + pkl.x), __ldg(dc + pij.x * nb + pkl.y)),
+                             fmaxf(__ldg(dc + pij.y * nb + pkl.x), __ldg(dc + pij.y * nb + pkl.y))));
+    return __ldg(c.bra.logq + bra) + __ldg(c.ket.logq + ket) + dmax >= d.log_cut;
+}
+
 // quartet g -> (range x, bra, ket)
 __device__ __forceinline__ void quartet_at(const ClassDev &c, int g, int &x, int &bra, int &ket) {
     int lo = 0, hi = c.nx;

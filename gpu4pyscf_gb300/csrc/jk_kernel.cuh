@@ -89,7 +89,48 @@ rys_class_kernel(EngineDev d, ClassDev c, int ntiles_static)
     const int total = MODE == MODE_JK ? c.q_off[c.nx] : 0;
     if (MODE == MODE_JK) ntiles = (total + QB - 1) / QB;
 
-    for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
+    // Work acquisition.  J/K mode: the block screens the class's quartets in
+    // chunks of candidates and keeps the ones that pass in a shared queue, so
+    // every batch of QB slots is full.  Schwarz mode: fixed tiles of pairs.
+    __shared__ int bq[MODE == MODE_JK ? QB + JK_THREADS : 1];
+    __shared__ int wcnt[JK_THREADS / 32];
+    constexpr int CHB = 4 * JK_THREADS;
+    int chunk = blockIdx.x;
+    int cur = chunk * CHB, cend = min(total, cur + CHB);
+    int nq = 0;
+    for (;;) {
+        int take = 0;
+        if (MODE == MODE_JK) {
+            bool done = false;
+            for (;;) {
+                while (nq < QB && cur < cend) {
+                    const int cand = cur + tid;
+                    const bool okc = cand < cend && quartet_passes(d, c, cand);
+                    const unsigned m = __ballot_sync(0xffffffffu, okc);
+                    if ((tid & 31) == 0) wcnt[tid >> 5] = __popc(m);
+                    __syncthreads();
+                    int off = 0, tot = 0;
+#pragma unroll
+                    for (int w = 0; w < JK_THREADS / 32; ++w) {
+                        if (w < (tid >> 5)) off += wcnt[w];
+                        tot += wcnt[w];
+                    }
+                    if (okc) bq[nq + off + __popc(m & ((1u << (tid & 31)) - 1u))] = cand;
+                    nq += tot;
+                    cur += JK_THREADS;
+                    __syncthreads();
+                }
+                if (nq > 0) break;
+                chunk += gridDim.x;
+                if (chunk * CHB >= total) { done = true; break; }
+                cur = chunk * CHB;
+                cend = min(total, cur + CHB);
+            }
+            if (done) break;
+            take = min(nq, QB);
+        } else {
+            if (chunk >= ntiles) break;
+        }
         // ---- slot setup -------------------------------------------------
         int nst = 0;
         if (tid < QB) {
@@ -98,27 +139,19 @@ rys_class_kernel(EngineDev d, ClassDev c, int ntiles_static)
             int bra = 0, ket = 0;
             bool ok;
             if (MODE == MODE_JK) {
-                const int g = tile * QB + tid;
-                ok = g < total;
+                const int cand = tid < take ? bq[tid] : -1;
+                ok = cand >= 0;
                 int xk;
-                if (ok) quartet_at(c, g, xk, bra, ket);
+                if (ok) quartet_at(c, cand, xk, bra, ket);
             } else {
-                bra = tile * QB + tid;
+                bra = chunk * QB + tid;
                 ket = bra;
                 ok = bra < c.bra.n;
             }
             if (ok) {
                 int2 pij = c.bra.ij[bra];
                 int2 pkl = c.ket.ij[ket];
-                if (MODE == MODE_JK) {
-                    const float *dc = d.dm_cond;
-                    int nb = d.nbas;
-                    float dmax = fmaxf(fmaxf(dc[pij.x * nb + pij.y], dc[pkl.x * nb + pkl.y]),
-                                       fmaxf(fmaxf(dc[pij.x * nb + pkl.x], dc[pij.x * nb + pkl.y]),
-                                             fmaxf(dc[pij.y * nb + pkl.x], dc[pij.y * nb + pkl.y])));
-                    ok = c.bra.logq[bra] + c.ket.logq[ket] + dmax >= d.log_cut;
-                }
-                if (ok) {
+                {
                     si.valid = 1;
                     si.ish = pij.x; si.jsh = pij.y; si.ksh = pkl.x; si.lsh = pkl.y;
                     si.pb_off = c.bra.prim_off[bra];
@@ -147,6 +180,17 @@ rys_class_kernel(EngineDev d, ClassDev c, int ntiles_static)
                 atomicAdd(d.counters + 2 * c.class_id, 1ull);
                 atomicAdd(d.counters + 2 * c.class_id + 1, (unsigned long long)si.nsteps);
             }
+        }
+        if (MODE == MODE_JK) {
+            // drop the taken entries from the queue
+            __syncthreads();
+            const int rem = nq - take;
+            const int t = tid < rem ? bq[take + tid] : 0;
+            __syncthreads();
+            if (tid < rem) bq[tid] = t;
+            nq = rem;
+        } else {
+            chunk += gridDim.x;
         }
         nst = __reduce_max_sync(0xffffffffu, nst);
         if ((tid & 31) == 0) wmax[tid >> 5] = nst;

@@ -110,24 +110,44 @@ rys_lean_kernel(EngineDev d, ClassDev c, int unused)
     constexpr int NFI = S::NFI, NFJ = S::NFJ, NFK = S::NFK, NFL = S::NFL;
     const int total = c.q_off[c.nx];
     const int lane = threadIdx.x & 31;
-    const int stride = gridDim.x * blockDim.x;
-    // warp-uniform loop: lane 0 of every iteration holds a valid quartet
-    for (int g0 = blockIdx.x * blockDim.x + (threadIdx.x & ~31); g0 < total; g0 += stride) {
-        const int g = g0 + lane;
+    // Per-warp compaction queue: the warp screens candidates 32 at a time and
+    // runs only quartets that pass, 32 per iteration.
+    __shared__ int queue[LEAN_THREADS / 32][64];
+    int *wq = queue[threadIdx.x >> 5];
+    constexpr int CHUNK = 1024;  // candidates per warp assignment
+    const int warp_id = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int nwarps = (gridDim.x * blockDim.x) >> 5;
+    for (int chunk = warp_id; chunk * CHUNK < total; chunk += nwarps) {
+      int cur = chunk * CHUNK;
+      const int cend = min(total, cur + CHUNK);
+      int nq = 0;
+      while (true) {
+        while (nq < 32 && cur < cend) {
+            const int cand = cur + lane;
+            const bool ok = cand < cend && quartet_passes(d, c, cand);
+            const unsigned m = __ballot_sync(0xffffffffu, ok);
+            if (ok) wq[nq + __popc(m & ((1u << lane) - 1u))] = cand;
+            nq += __popc(m);
+            cur += 32;
+            __syncwarp();
+        }
+        if (nq == 0) break;
+        const int take = min(nq, 32);
+        const int mine = lane < take ? wq[lane] : -1;
+        __syncwarp();
+        if (nq > 32) {
+            int t = lane < nq - 32 ? wq[32 + lane] : 0;
+            __syncwarp();
+            if (lane < nq - 32) wq[lane] = t;
+        }
+        nq -= take;
+        __syncwarp();
+        bool valid = mine >= 0;
         int xk, ib, ket;
-        quartet_at(c, g < total ? g : g0, xk, ib, ket);
-        bool valid = g < total;
+        quartet_at(c, valid ? mine : __shfl_sync(0xffffffffu, mine, 0), xk, ib, ket);
         const int2 pij = c.bra.ij[ib];
         int2 pkl = make_int2(0, 0);
-        if (valid) {
-            pkl = c.ket.ij[ket];
-            const float *dc = d.dm_cond;
-            const int nb = d.nbas;
-            float dmax = fmaxf(fmaxf(dc[pij.x * nb + pij.y], dc[pkl.x * nb + pkl.y]),
-                               fmaxf(fmaxf(dc[pij.x * nb + pkl.x], dc[pij.x * nb + pkl.y]),
-                                     fmaxf(dc[pij.y * nb + pkl.x], dc[pij.y * nb + pkl.y])));
-            valid = c.bra.logq[ib] + c.ket.logq[ket] + dmax >= d.log_cut;
-        }
+        if (valid) pkl = c.ket.ij[ket];
         // the J block of the bra pair can be summed across the warp when all
         // its lanes share the bra
         const bool same_bra = __all_sync(0xffffffffu, ib == __shfl_sync(0xffffffffu, ib, 0));
@@ -329,6 +349,7 @@ rys_lean_kernel(EngineDev d, ClassDev c, int unused)
                     }
             }
         }
+      }
     }
 }
 
