@@ -143,8 +143,10 @@ rys_lean_kernel(EngineDev d, ClassDev c, int unused)
         nq -= take;
         __syncwarp();
         bool valid = mine >= 0;
+        // lane 0 always holds a quartet; idle lanes borrow its indices
+        const int lead = __shfl_sync(0xffffffffu, mine, 0);
         int xk, ib, ket;
-        quartet_at(c, valid ? mine : __shfl_sync(0xffffffffu, mine, 0), xk, ib, ket);
+        quartet_at(c, valid ? mine : lead, xk, ib, ket);
         const int2 pij = c.bra.ij[ib];
         int2 pkl = make_int2(0, 0);
         if (valid) pkl = c.ket.ij[ket];
