@@ -82,7 +82,24 @@ struct ClassDev {
     const int *q_off;         // [nx + 1] quartet offsets
     const int *ket_begin;     // [nx]
     const int *ket_end;       // [nx]
+    int *work;                // range counter of this launch (zeroed per build)
 };
+
+// Screening of (bra, ket) of a class: q_ij q_kl times the largest of the six
+// density blocks the quartet touches against the cutoff
+// (gpu4pyscf/lib/gvhf-rys/create_tasks.cu:152-162).
+__device__ __forceinline__ bool pair_passes(const EngineDev &d, const ClassDev &c, int bra, int ket) {
+    const int2 pij = c.bra.ij[bra], pkl = c.ket.ij[ket];
+    const float *dc = d.dm_cond;
+    const int nb = d.nbas;
+    float dmax = fmaxf(fmaxf(__ldg(dc + pij.x * nb + pij.y), __ldg(dc + pkl.x * nb + pkl.y)),
+                       fmaxf(fmaxf(__ldg(dc + pij.x * nb + pkl.x), __ldg(dc + pij.x * nb + pkl.y)),
+                             fmaxf(__ldg(dc + pij.y * nb + pkl.x), __ldg(dc + pij.y * nb + pkl.y))));
+    return __ldg(c.bra.logq + bra) + __ldg(c.ket.logq + ket) + dmax >= d.log_cut;
+}
+
+// ranges taken per grab of the work counter
+#define JK_RANGE_GRAB 4
 
 __device__ __forceinline__ void quartet_at(const ClassDev &c, int g, int &x, int &bra, int &ket);
 

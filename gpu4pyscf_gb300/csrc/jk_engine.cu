@@ -282,6 +282,7 @@ struct jk_opt {
     double *dmj = nullptr, *dmk = nullptr, *jt = nullptr, *kt = nullptr;
     float *dmj_f = nullptr, *dmk_f = nullptr;
     unsigned long long *counters = nullptr;
+    int *work = nullptr;                 // [2 * NQCLASS] range counters of the class launches
     std::vector<void *> owned;
     // per-class timing (diagnostics)
     bool time_classes = false;
@@ -684,6 +685,7 @@ int jk_opt_create(const int32_t *atm, int natm, const int32_t *bas, int nbas, co
     if (int e = own_alloc(o, &o->dm_cond, (size_t)nbas * nbas)) return bail(e);
     if (int e = own_alloc(o, &o->dm_max, 1)) return bail(e);
     if (int e = own_alloc(o, &o->counters, 4 * NQCLASS)) return bail(e);
+    if (int e = own_alloc(o, &o->work, 2 * NQCLASS)) return bail(e);
     *out = o;
     return 0;
 }
@@ -739,6 +741,7 @@ int jk_build(jk_opt *o, const double *dm, int n_dm, int nao, int hermi, int with
     CK(cudaGetLastError());
     if (with_j) CK(cudaMemsetAsync(o->jt, 0, sizeof(double) * nn * n_dm, st));
     if (with_k) CK(cudaMemsetAsync(o->kt, 0, sizeof(double) * nn * n_dmk, st));
+    CK(cudaMemsetAsync(o->work, 0, sizeof(int) * 2 * NQCLASS, st));
     const bool want_stats = stats != nullptr;
     if (want_stats) CK(cudaMemsetAsync(o->counters, 0, sizeof(unsigned long long) * 4 * NQCLASS, st));
 
@@ -775,6 +778,7 @@ int jk_build(jk_opt *o, const double *dm, int n_dm, int nao, int hermi, int with
         if (!d.with_j && !d.with_k) break;
         c.class_id = q;
         d.counters = want_stats ? o->counters : nullptr;
+        c.work = o->work + 2 * q;
         c.q_off = o->off64[q]; c.ket_begin = o->kb64[q]; c.ket_end = o->ke64[q];
         if (o->time_classes) { o->ev_slot.push_back(2 * q); CK(cudaEventRecord(o->ev[2 * (o->ev_slot.size() - 1)], st)); }
         if (int er = launch_class(e.k64, grid_for(o, upper, e.lean), e.smem64, d, c, 0, st, e.threads64)) return er;
@@ -782,6 +786,7 @@ int jk_build(jk_opt *o, const double *dm, int n_dm, int nao, int hermi, int with
         ++launches;
         if (mixed) {
             c.class_id = NQCLASS + q;  // FP32 counters in the second half
+            c.work = o->work + 2 * q + 1;
             c.q_off = o->off32[q]; c.ket_begin = o->kb32[q]; c.ket_end = o->ke32[q];
             long long up32 = (long long)o->npairs[a] * ((o->npairs[b] + e.qb32 - 1) / e.qb32 + o->nbk[b]);
             if (o->time_classes) { o->ev_slot.push_back(2 * q + 1); CK(cudaEventRecord(o->ev[2 * (o->ev_slot.size() - 1)], st)); }
@@ -894,7 +899,8 @@ extern "C" int jk_build_noalloc(jk_opt *o, const double *dm, int n_dm, int nao, 
     size_t off_dmkf = off_dmjf + (mixed ? align256(sizeof(float) * nn * n_dm) : 0);
     size_t off_cond = off_dmkf + (mixed ? align256(sizeof(float) * nn * n_dmk) : 0);
     size_t off_max = off_cond + align256(sizeof(float) * (size_t)o->nbas * o->nbas);
-    size_t need = off_max + 256;
+    size_t off_work = off_max + 256;
+    size_t need = off_work + align256(sizeof(int) * 2 * NQCLASS);
     if (need > JK_NOALLOC_SCRATCH_BYTES) {
         char msg[256];
         std::snprintf(msg, sizeof(msg),
@@ -910,6 +916,7 @@ extern "C" int jk_build_noalloc(jk_opt *o, const double *dm, int n_dm, int nao, 
     float *dmj_f = mixed ? (float *)(b + off_dmjf) : nullptr;
     float *dmk_f = mixed ? (float *)(b + off_dmkf) : nullptr;
     float *dm_cond = (float *)(b + off_cond), *dm_max = (float *)(b + off_max);
+    int *work = (int *)(b + off_work);
     cudaStream_t st = (cudaStream_t)stream;
     {
         int grid = (int)std::min<size_t>((nn * n_dm + 255) / 256, (size_t)o->sm_count * 8);
@@ -929,6 +936,7 @@ extern "C" int jk_build_noalloc(jk_opt *o, const double *dm, int n_dm, int nao, 
     // the accumulators keep the previous call's contents: clear them
     CK(cudaMemsetAsync(jt, 0, sizeof(double) * nn * n_dm, st));
     CK(cudaMemsetAsync(kt, 0, sizeof(double) * nn * n_dmk, st));
+    CK(cudaMemsetAsync(work, 0, sizeof(int) * 2 * NQCLASS, st));
     EngineDev d = base_engine(o);
     d.dm_cond = dm_cond;
     d.dmj = dmj; d.dmk = dmk; d.dmj_f = dmj_f; d.dmk_f = dmk_f;
@@ -952,11 +960,13 @@ extern "C" int jk_build_noalloc(jk_opt *o, const double *dm, int n_dm, int nao, 
             c.nbk = o->nbk[bcls];
             c.nx = o->npairs[a] * o->nbk[bcls];
             c.class_id = q;
+            c.work = work + 2 * q;
             c.q_off = o->off64[q]; c.ket_begin = o->kb64[q]; c.ket_end = o->ke64[q];
             long long upper = (long long)o->npairs[a] * ((o->npairs[bcls] + e.qb64 - 1) / e.qb64 + o->nbk[bcls]);
             if (int er = launch_class(e.k64, grid_for(o, upper, e.lean), e.smem64, d, c, 0, st, e.threads64)) return er;
             if (mixed) {
                 c.class_id = NQCLASS + q;
+                c.work = work + 2 * q + 1;
                 c.q_off = o->off32[q]; c.ket_begin = o->kb32[q]; c.ket_end = o->ke32[q];
                 long long up32 = (long long)o->npairs[a] * ((o->npairs[bcls] + e.qb32 - 1) / e.qb32 + o->nbk[bcls]);
                 if (int er = launch_class(e.k32, grid_for(o, up32, e.lean), e.smem32, d, c, 0, st, e.threads32)) return er;

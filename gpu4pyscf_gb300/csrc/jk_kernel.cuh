@@ -85,48 +85,57 @@ rys_class_kernel(EngineDev d, ClassDev c, int ntiles_static)
         }
     }
 
-    int ntiles = ntiles_static;
-    const int total = MODE == MODE_JK ? c.q_off[c.nx] : 0;
-    if (MODE == MODE_JK) ntiles = (total + QB - 1) / QB;
+    const int ntiles = ntiles_static;
 
-    // Work acquisition.  J/K mode: the block screens the class's quartets in
-    // chunks of candidates and keeps the ones that pass in a shared queue, so
-    // every batch of QB slots is full.  Schwarz mode: fixed tiles of pairs.
-    __shared__ int bq[MODE == MODE_JK ? QB + JK_THREADS : 1];
+    // Work acquisition.  J/K mode: the block takes (ket bucket, bra) ket
+    // ranges from the launch's work counter, screens their kets and keeps
+    // the quartets that pass in a shared queue, so every batch of QB slots is
+    // full.  Schwarz mode: fixed tiles of pairs.
+    __shared__ int2 bq[MODE == MODE_JK ? QB + JK_THREADS : 1];
     __shared__ int wcnt[JK_THREADS / 32];
-    constexpr int CHB = 4 * JK_THREADS;
+    __shared__ int s_base;
     int chunk = blockIdx.x;
-    int cur = chunk * CHB, cend = min(total, cur + CHB);
+    int xcur = 0, xend = 0, kcur = 0, kend = 0, bcur = 0;
+    bool exhausted = false;
     int nq = 0;
     for (;;) {
         int take = 0;
         if (MODE == MODE_JK) {
-            bool done = false;
-            for (;;) {
-                while (nq < QB && cur < cend) {
-                    const int cand = cur + tid;
-                    const bool okc = cand < cend && quartet_passes(d, c, cand);
-                    const unsigned m = __ballot_sync(0xffffffffu, okc);
-                    if ((tid & 31) == 0) wcnt[tid >> 5] = __popc(m);
-                    __syncthreads();
-                    int off = 0, tot = 0;
-#pragma unroll
-                    for (int w = 0; w < JK_THREADS / 32; ++w) {
-                        if (w < (tid >> 5)) off += wcnt[w];
-                        tot += wcnt[w];
+            while (nq < QB && !exhausted) {
+                if (kcur >= kend) {
+                    if (xcur + 1 < xend) {
+                        ++xcur;
+                    } else {
+                        if (tid == 0) s_base = atomicAdd(c.work, JK_RANGE_GRAB);
+                        __syncthreads();
+                        const int base = s_base;
+                        __syncthreads();
+                        if (base >= c.nx) { exhausted = true; break; }
+                        xcur = base;
+                        xend = min(c.nx, base + JK_RANGE_GRAB);
                     }
-                    if (okc) bq[nq + off + __popc(m & ((1u << (tid & 31)) - 1u))] = cand;
-                    nq += tot;
-                    cur += JK_THREADS;
-                    __syncthreads();
+                    kcur = __ldg(c.ket_begin + xcur);
+                    kend = __ldg(c.ket_end + xcur);
+                    bcur = xcur % c.bra.n;
+                    continue;
                 }
-                if (nq > 0) break;
-                chunk += gridDim.x;
-                if (chunk * CHB >= total) { done = true; break; }
-                cur = chunk * CHB;
-                cend = min(total, cur + CHB);
+                const int kk = kcur + tid;
+                const bool okc = kk < kend && pair_passes(d, c, bcur, kk);
+                const unsigned m = __ballot_sync(0xffffffffu, okc);
+                if ((tid & 31) == 0) wcnt[tid >> 5] = __popc(m);
+                __syncthreads();
+                int off = 0, tot = 0;
+#pragma unroll
+                for (int w = 0; w < JK_THREADS / 32; ++w) {
+                    if (w < (tid >> 5)) off += wcnt[w];
+                    tot += wcnt[w];
+                }
+                if (okc) bq[nq + off + __popc(m & ((1u << (tid & 31)) - 1u))] = make_int2(bcur, kk);
+                nq += tot;
+                kcur += JK_THREADS;
+                __syncthreads();
             }
-            if (done) break;
+            if (nq == 0) break;
             take = min(nq, QB);
         } else {
             if (chunk >= ntiles) break;
@@ -139,10 +148,8 @@ rys_class_kernel(EngineDev d, ClassDev c, int ntiles_static)
             int bra = 0, ket = 0;
             bool ok;
             if (MODE == MODE_JK) {
-                const int cand = tid < take ? bq[tid] : -1;
-                ok = cand >= 0;
-                int xk;
-                if (ok) quartet_at(c, cand, xk, bra, ket);
+                ok = tid < take;
+                if (ok) { bra = bq[tid].x; ket = bq[tid].y; }
             } else {
                 bra = chunk * QB + tid;
                 ket = bra;
@@ -185,7 +192,7 @@ rys_class_kernel(EngineDev d, ClassDev c, int ntiles_static)
             // drop the taken entries from the queue
             __syncthreads();
             const int rem = nq - take;
-            const int t = tid < rem ? bq[take + tid] : 0;
+            const int2 t = tid < rem ? bq[take + tid] : make_int2(0, 0);
             __syncthreads();
             if (tid < rem) bq[tid] = t;
             nq = rem;

@@ -1,9 +1,9 @@
 // Register-resident Rys J/K kernel for the small angular classes.
 //
-// One thread owns one shell quartet from start to end: no shared memory and
-// no barriers.  Threads take consecutive quartets of the class's quartet
-// numbering (ket-bucket major), so the lanes of a warp are all busy and run
-// the same number of ket primitive iterations.  Per primitive quartet and root the
+// One thread owns one shell quartet from start to end, with no block
+// barriers.  Each warp takes (ket bucket, bra) ranges from a work counter,
+// screens their kets and queues the survivors, so its 32 lanes run 32
+// quartets with the same ket primitive count at a time.  Per primitive quartet and root the
 // 2D integrals of the three axes live in registers (fully unrolled vertical
 // recurrence and horizontal transfers), the Cartesian ERI block accumulates
 // in registers, and after the primitive loops the thread contracts its block
@@ -108,45 +108,58 @@ rys_lean_kernel(EngineDev d, ClassDev c, int unused)
     using S = LeanShape<LI, LJ, LK, LL>;
     constexpr int NR = S::NR, NF = S::NF, GS = S::GS, GSKL = S::GSKL;
     constexpr int NFI = S::NFI, NFJ = S::NFJ, NFK = S::NFK, NFL = S::NFL;
-    const int total = c.q_off[c.nx];
     const int lane = threadIdx.x & 31;
-    // Per-warp compaction queue: the warp screens candidates 32 at a time and
-    // runs only quartets that pass, 32 per iteration.
-    __shared__ int queue[LEAN_THREADS / 32][64];
-    int *wq = queue[threadIdx.x >> 5];
-    constexpr int CHUNK = 1024;  // candidates per warp assignment
-    const int warp_id = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    const int nwarps = (gridDim.x * blockDim.x) >> 5;
-    for (int chunk = warp_id; chunk * CHUNK < total; chunk += nwarps) {
-      int cur = chunk * CHUNK;
-      const int cend = min(total, cur + CHUNK);
-      int nq = 0;
-      while (true) {
-        while (nq < 32 && cur < cend) {
-            const int cand = cur + lane;
-            const bool ok = cand < cend && quartet_passes(d, c, cand);
+    // Per-warp work: the warp takes JK_RANGE_GRAB (bucket, bra) ket ranges at
+    // a time from the launch's counter, screens their kets 32 at a time and
+    // queues the quartets that pass; each iteration runs 32 queued quartets.
+    __shared__ int2 queue[LEAN_THREADS / 32][64];
+    int2 *wq = queue[threadIdx.x >> 5];
+    int xcur = 0, xend = 0, kcur = 0, kend = 0, bcur = 0;
+    bool exhausted = false;
+    int nq = 0;
+    while (true) {
+        while (nq < 32 && !exhausted) {
+            if (kcur >= kend) {
+                if (xcur + 1 < xend) {
+                    ++xcur;
+                } else {
+                    int base = 0;
+                    if (lane == 0) base = atomicAdd(c.work, JK_RANGE_GRAB);
+                    base = __shfl_sync(0xffffffffu, base, 0);
+                    if (base >= c.nx) { exhausted = true; break; }
+                    xcur = base;
+                    xend = min(c.nx, base + JK_RANGE_GRAB);
+                }
+                kcur = __ldg(c.ket_begin + xcur);
+                kend = __ldg(c.ket_end + xcur);
+                bcur = xcur % c.bra.n;
+                continue;
+            }
+            const int kk = kcur + lane;
+            const bool ok = kk < kend && pair_passes(d, c, bcur, kk);
             const unsigned m = __ballot_sync(0xffffffffu, ok);
-            if (ok) wq[nq + __popc(m & ((1u << lane) - 1u))] = cand;
+            if (ok) wq[nq + __popc(m & ((1u << lane) - 1u))] = make_int2(bcur, kk);
             nq += __popc(m);
-            cur += 32;
+            kcur += 32;
             __syncwarp();
         }
         if (nq == 0) break;
         const int take = min(nq, 32);
-        const int mine = lane < take ? wq[lane] : -1;
+        const int2 mine = lane < take ? wq[lane] : make_int2(-1, -1);
         __syncwarp();
         if (nq > 32) {
-            int t = lane < nq - 32 ? wq[32 + lane] : 0;
+            int2 t = lane < nq - 32 ? wq[32 + lane] : make_int2(0, 0);
             __syncwarp();
             if (lane < nq - 32) wq[lane] = t;
         }
         nq -= take;
         __syncwarp();
-        bool valid = mine >= 0;
+        const bool valid = mine.x >= 0;
         // lane 0 always holds a quartet; idle lanes borrow its indices
-        const int lead = __shfl_sync(0xffffffffu, mine, 0);
-        int xk, ib, ket;
-        quartet_at(c, valid ? mine : lead, xk, ib, ket);
+        const int lead_b = __shfl_sync(0xffffffffu, mine.x, 0);
+        const int lead_k = __shfl_sync(0xffffffffu, mine.y, 0);
+        const int ib = valid ? mine.x : lead_b;
+        const int ket = valid ? mine.y : lead_k;
         const int2 pij = c.bra.ij[ib];
         int2 pkl = make_int2(0, 0);
         if (valid) pkl = c.ket.ij[ket];
@@ -351,7 +364,6 @@ rys_lean_kernel(EngineDev d, ClassDev c, int unused)
                     }
             }
         }
-      }
     }
 }
 
