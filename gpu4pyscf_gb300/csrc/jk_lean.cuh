@@ -9,8 +9,8 @@
 // in registers, and after the primitive loops the thread contracts its block
 // with the six density blocks.  The J block of the bra pair, common to the
 // warp when all its lanes share the bra pair, is summed across the warp with
-// shuffles before one atomic add per element; the other five blocks go out
-// with one atomic add per element.
+// shuffles before one atomic add per element; the four K blocks go out with
+// one atomic add per distinct address of the warp, J_kl directly.
 #pragma once
 #include "jk_device.cuh"
 #include "rys_roots.cuh"
@@ -91,6 +91,25 @@ __device__ __forceinline__ void rys2d(Real i00, Real c00, Real cp00, Real b00, R
         }
 }
 
+// Atomic add aggregated over the lanes of a warp that target the same
+// address: one atomic per distinct address (lanes with addr == nullptr add
+// nothing).  All 32 lanes must call it together.
+__device__ __forceinline__ void warp_agg_add(double *addr, double v, double *buf, int lane) {
+    const unsigned peers = __match_any_sync(0xffffffffu, (unsigned long long)addr);
+    buf[lane] = v;
+    __syncwarp();
+    if (addr != nullptr && lane == __ffs(peers) - 1) {
+        double s = 0.;
+        unsigned m = peers;
+        while (m) {
+            s += buf[__ffs(m) - 1];
+            m &= m - 1;
+        }
+        if (s != 0.) atomicAdd(addr, s);
+    }
+    __syncwarp();
+}
+
 template <typename Real> struct LeanIO;
 template <> struct LeanIO<double> {
     static __device__ __forceinline__ const double *dj(const EngineDev &d) { return d.dmj; }
@@ -113,7 +132,9 @@ rys_lean_kernel(EngineDev d, ClassDev c, int unused)
     // a time from the launch's counter, screens their kets 32 at a time and
     // queues the quartets that pass; each iteration runs 32 queued quartets.
     __shared__ int2 queue[LEAN_THREADS / 32][64];
+    __shared__ double aggbuf[LEAN_THREADS / 32][32];
     int2 *wq = queue[threadIdx.x >> 5];
+    double *ab_buf = aggbuf[threadIdx.x >> 5];
     int xcur = 0, xend = 0, kcur = 0, kend = 0, bcur = 0;
     bool exhausted = false;
     int nq = 0;
@@ -299,7 +320,9 @@ rys_lean_kernel(EngineDev d, ClassDev c, int unused)
                 }
             }
         }
-        if (d.with_k && valid) {
+        if (d.with_k) {
+            // lanes whose kets share a shell hit the same K elements: add
+            // through warp aggregation (idle lanes contribute nothing)
             for (int idm = 0; idm < d.n_dmk; ++idm) {
                 const Real *Dm = LeanIO<Real>::dk(d) + idm * nn;
                 double *V = d.vk + idm * nn;
@@ -327,7 +350,7 @@ rys_lean_kernel(EngineDev d, ClassDev c, int unused)
                         for (int b = 0; b < NFJ; ++b)
 #pragma unroll
                             for (int dd = 0; dd < NFL; ++dd) s += acc[((a * NFJ + b) * NFK + cc) * NFL + dd] * djl[b * NFL + dd];
-                        atomicAdd(V + (size_t)(ai + a) * nao + ak + cc, (double)(fac * s));
+                        warp_agg_add(valid ? V + (size_t)(ai + a) * nao + ak + cc : nullptr, (double)(fac * s), ab_buf, lane);
                     }
 #pragma unroll
                 for (int a = 0; a < NFI; ++a)
@@ -338,7 +361,7 @@ rys_lean_kernel(EngineDev d, ClassDev c, int unused)
                         for (int b = 0; b < NFJ; ++b)
 #pragma unroll
                             for (int cc = 0; cc < NFK; ++cc) s += acc[((a * NFJ + b) * NFK + cc) * NFL + dd] * djk[b * NFK + cc];
-                        atomicAdd(V + (size_t)(ai + a) * nao + al + dd, (double)(fac * s));
+                        warp_agg_add(valid ? V + (size_t)(ai + a) * nao + al + dd : nullptr, (double)(fac * s), ab_buf, lane);
                     }
 #pragma unroll
                 for (int b = 0; b < NFJ; ++b)
@@ -349,7 +372,7 @@ rys_lean_kernel(EngineDev d, ClassDev c, int unused)
                         for (int a = 0; a < NFI; ++a)
 #pragma unroll
                             for (int dd = 0; dd < NFL; ++dd) s += acc[((a * NFJ + b) * NFK + cc) * NFL + dd] * dil[a * NFL + dd];
-                        atomicAdd(V + (size_t)(aj + b) * nao + ak + cc, (double)(fac * s));
+                        warp_agg_add(valid ? V + (size_t)(aj + b) * nao + ak + cc : nullptr, (double)(fac * s), ab_buf, lane);
                     }
 #pragma unroll
                 for (int b = 0; b < NFJ; ++b)
@@ -360,7 +383,7 @@ rys_lean_kernel(EngineDev d, ClassDev c, int unused)
                         for (int a = 0; a < NFI; ++a)
 #pragma unroll
                             for (int cc = 0; cc < NFK; ++cc) s += acc[((a * NFJ + b) * NFK + cc) * NFL + dd] * dik[a * NFK + cc];
-                        atomicAdd(V + (size_t)(aj + b) * nao + al + dd, (double)(fac * s));
+                        warp_agg_add(valid ? V + (size_t)(aj + b) * nao + al + dd : nullptr, (double)(fac * s), ab_buf, lane);
                     }
             }
         }
