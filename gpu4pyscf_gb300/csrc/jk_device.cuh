@@ -70,16 +70,16 @@ struct EngineDev {
 // Work of one quartet class.  The ket list is split into buckets of equal
 // primitive-pair count (each bucket sorted by Schwarz factor, descending);
 // x = bucket * bra.n + bra indexes the ket range [ket_begin[x], ket_end[x]),
-// and the class's quartets are numbered consecutively through the x ranges:
-// quartet g lies in range x with q_off[x] <= g < q_off[x + 1], so
-// neighbouring quartets share primitive counts.
+// and each range is cut into work units of JK_KCHUNK kets numbered through
+// the class (range x holds units q_off[x] .. q_off[x+1]-1), so consecutive
+// units share primitive counts.
 struct ClassDev {
     PairList bra, ket;
     int same;                 // bra list == ket list
     int class_id;
     int nbk;                  // ket buckets
     int nx;                   // bra.n * nbk
-    const int *q_off;         // [nx + 1] quartet offsets
+    const int *q_off;         // [nx + 1] work-unit offsets (units of JK_KCHUNK kets)
     const int *ket_begin;     // [nx]
     const int *ket_end;       // [nx]
     int *work;                // range counter of this launch (zeroed per build)
@@ -98,8 +98,21 @@ __device__ __forceinline__ bool pair_passes(const EngineDev &d, const ClassDev &
     return __ldg(c.bra.logq + bra) + __ldg(c.ket.logq + ket) + dmax >= d.log_cut;
 }
 
-// ranges taken per grab of the work counter
-#define JK_RANGE_GRAB 4
+// kets per work unit: a range [ket_begin[x], ket_end[x]) is cut into units
+// of JK_KCHUNK kets, numbered through the class by q_off (unit prefix sums)
+#define JK_KCHUNK 64
+
+// work unit w -> range x and its ket interval [k0, k1)
+__device__ __forceinline__ void unit_at(const ClassDev &c, int w, int &x, int &k0, int &k1) {
+    int lo = 0, hi = c.nx;
+    while (hi - lo > 1) {
+        int mid = (lo + hi) >> 1;
+        if (__ldg(c.q_off + mid) <= w) lo = mid; else hi = mid;
+    }
+    x = lo;
+    k0 = __ldg(c.ket_begin + lo) + (w - __ldg(c.q_off + lo)) * JK_KCHUNK;
+    k1 = min(__ldg(c.ket_end + lo), k0 + JK_KCHUNK);
+}
 
 __device__ __forceinline__ void quartet_at(const ClassDev &c, int g, int &x, int &bra, int &ket);
 

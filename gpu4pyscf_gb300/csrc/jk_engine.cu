@@ -158,7 +158,7 @@ __device__ int count_ge(const float *q, int n, float thr) {
 
 // Per (ket bucket, bra pair): the ket range passing q_ij q_kl max|D| >= tol
 // and, in mixed mode, its split into an FP64 head and an FP32 tail; the
-// counts are the quartets of each range, scanned into quartet offsets.
+// counts are the work units of each range, scanned into unit offsets.
 __global__ void plan_kernel(const PlanClass *pcs, int npc, int total, const float *dm_max,
                             float log_cut, float log_split, int mixed) {
     int g = blockIdx.x * blockDim.x + threadIdx.x;
@@ -183,10 +183,10 @@ __global__ void plan_kernel(const PlanClass *pcs, int npc, int total, const floa
     }
     p.kb64[x] = b0;
     p.ke64[x] = mid;
-    p.cnt64[x] = mid - b0;
+    p.cnt64[x] = (mid - b0 + JK_KCHUNK - 1) / JK_KCHUNK;
     p.kb32[x] = mid;
     p.ke32[x] = end;
-    p.cnt32[x] = mixed ? end - mid : 0;
+    p.cnt32[x] = mixed ? (end - mid + JK_KCHUNK - 1) / JK_KCHUNK : 0;
 }
 
 struct ScanJob { const int *cnt; int *off; int n; };

@@ -87,15 +87,16 @@ rys_class_kernel(EngineDev d, ClassDev c, int ntiles_static)
 
     const int ntiles = ntiles_static;
 
-    // Work acquisition.  J/K mode: the block takes (ket bucket, bra) ket
-    // ranges from the launch's work counter, screens their kets and keeps
+    // Work acquisition.  J/K mode: the block takes work units (JK_KCHUNK kets
+    // of one (ket bucket, bra) range) from the launch's counter, screens them and keeps
     // the quartets that pass in a shared queue, so every batch of QB slots is
     // full.  Schwarz mode: fixed tiles of pairs.
     __shared__ int2 bq[MODE == MODE_JK ? QB + JK_THREADS : 1];
     __shared__ int wcnt[JK_THREADS / 32];
     __shared__ int s_base;
     int chunk = blockIdx.x;
-    int xcur = 0, xend = 0, kcur = 0, kend = 0, bcur = 0;
+    const int nunits = MODE == MODE_JK ? __ldg(c.q_off + c.nx) : 0;
+    int kcur = 0, kend = 0, bcur = 0;
     bool exhausted = false;
     int nq = 0;
     for (;;) {
@@ -103,20 +104,14 @@ rys_class_kernel(EngineDev d, ClassDev c, int ntiles_static)
         if (MODE == MODE_JK) {
             while (nq < QB && !exhausted) {
                 if (kcur >= kend) {
-                    if (xcur + 1 < xend) {
-                        ++xcur;
-                    } else {
-                        if (tid == 0) s_base = atomicAdd(c.work, JK_RANGE_GRAB);
-                        __syncthreads();
-                        const int base = s_base;
-                        __syncthreads();
-                        if (base >= c.nx) { exhausted = true; break; }
-                        xcur = base;
-                        xend = min(c.nx, base + JK_RANGE_GRAB);
-                    }
-                    kcur = __ldg(c.ket_begin + xcur);
-                    kend = __ldg(c.ket_end + xcur);
-                    bcur = xcur % c.bra.n;
+                    if (tid == 0) s_base = atomicAdd(c.work, 1);
+                    __syncthreads();
+                    const int w = s_base;
+                    __syncthreads();
+                    if (w >= nunits) { exhausted = true; break; }
+                    int xw;
+                    unit_at(c, w, xw, kcur, kend);
+                    bcur = xw % c.bra.n;
                     continue;
                 }
                 const int kk = kcur + tid;

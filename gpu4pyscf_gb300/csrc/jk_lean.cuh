@@ -128,32 +128,28 @@ rys_lean_kernel(EngineDev d, ClassDev c, int unused)
     constexpr int NR = S::NR, NF = S::NF, GS = S::GS, GSKL = S::GSKL;
     constexpr int NFI = S::NFI, NFJ = S::NFJ, NFK = S::NFK, NFL = S::NFL;
     const int lane = threadIdx.x & 31;
-    // Per-warp work: the warp takes JK_RANGE_GRAB (bucket, bra) ket ranges at
-    // a time from the launch's counter, screens their kets 32 at a time and
-    // queues the quartets that pass; each iteration runs 32 queued quartets.
+    // Per-warp work: the warp takes work units (JK_KCHUNK kets of one
+    // (bucket, bra) range) from the launch's counter, screens their kets 32 at
+    // a time and queues the quartets that pass; each iteration runs 32 queued
+    // quartets.
     __shared__ int2 queue[LEAN_THREADS / 32][64];
     __shared__ double aggbuf[LEAN_THREADS / 32][32];
     int2 *wq = queue[threadIdx.x >> 5];
     double *ab_buf = aggbuf[threadIdx.x >> 5];
-    int xcur = 0, xend = 0, kcur = 0, kend = 0, bcur = 0;
+    const int nunits = __ldg(c.q_off + c.nx);
+    int kcur = 0, kend = 0, bcur = 0;
     bool exhausted = false;
     int nq = 0;
     while (true) {
         while (nq < 32 && !exhausted) {
             if (kcur >= kend) {
-                if (xcur + 1 < xend) {
-                    ++xcur;
-                } else {
-                    int base = 0;
-                    if (lane == 0) base = atomicAdd(c.work, JK_RANGE_GRAB);
-                    base = __shfl_sync(0xffffffffu, base, 0);
-                    if (base >= c.nx) { exhausted = true; break; }
-                    xcur = base;
-                    xend = min(c.nx, base + JK_RANGE_GRAB);
-                }
-                kcur = __ldg(c.ket_begin + xcur);
-                kend = __ldg(c.ket_end + xcur);
-                bcur = xcur % c.bra.n;
+                int w = 0;
+                if (lane == 0) w = atomicAdd(c.work, 1);
+                w = __shfl_sync(0xffffffffu, w, 0);
+                if (w >= nunits) { exhausted = true; break; }
+                int xw;
+                unit_at(c, w, xw, kcur, kend);
+                bcur = xw % c.bra.n;
                 continue;
             }
             const int kk = kcur + lane;
