@@ -274,7 +274,31 @@ def run_gpu(args):
         lib.jk_opt_class_times(h, ms.ctypes.data, fl.ctypes.data, qq.ctypes.data,
                                *[x.ctypes.data for x in L])
         best_ms = np.minimum(best_ms, np.where(ms > 0, ms, np.inf))
+    # the same for the mixed build: FP32 class kernels (odd slots)
+    opt.precision, opt.split_thresh = 'mixed', args.split
+    opt._build(dms, 1, True, True, stats=True)
+    ms32 = np.full(2 * nq, np.inf)
+    fl32 = np.zeros(2 * nq, dtype=np.int64)
+    qq32 = np.zeros(2 * nq, dtype=np.int64)
+    for _ in range(2):
+        flush.zero_()
+        opt._build(dms, 1, True, True)
+        lib.jk_opt_class_times(h, ms.ctypes.data, fl32.ctypes.data, qq32.ctypes.data,
+                               *[x.ctypes.data for x in L])
+        ms32 = np.minimum(ms32, np.where(ms > 0, ms, np.inf))
+    ms32[~np.isfinite(ms32)] = 0.
+    opt.precision = 'fp64'
     lib.jk_opt_time_classes(h, 0)
+    fp32_classes = []
+    for q in range(nq):
+        if ms32[2 * q + 1] > 0:
+            fp32_classes.append(['(%d%d|%d%d)' % (L[0][q], L[1][q], L[2][q], L[3][q]),
+                                 round(float(ms32[2 * q + 1]), 4), int(qq32[2 * q + 1]),
+                                 round(float(ms32[2 * q]), 4), int(qq32[2 * q])])
+    fp32_classes.sort(key=lambda r: -r[1])
+    mixed['classes_top_fp32'] = fp32_classes[:8]
+    mixed['sum_fp32_class_ms'] = float(ms32[1::2].sum())
+    mixed['sum_fp64_class_ms'] = float(ms32[0::2].sum())
     best_ms[~np.isfinite(best_ms)] = 0.
     k = int(np.argmax(best_ms[0::2])) * 2
     peak64 = fma_peak(lib, 0)

@@ -284,6 +284,12 @@ struct jk_opt {
     unsigned long long *counters = nullptr;
     int *work = nullptr;                 // [2 * NQCLASS] range counters of the class launches
     std::vector<void *> owned;
+    // side streams: class kernels of one build run concurrently on them,
+    // forked from and joined back into the caller's stream with events
+    static constexpr int NSIDE = 4;
+    cudaStream_t side[NSIDE] = {};
+    cudaEvent_t fork_ev = nullptr;
+    cudaEvent_t join_ev[NSIDE] = {};
     // per-class timing (diagnostics)
     bool time_classes = false;
     std::vector<cudaEvent_t> ev;        // pairs of events
@@ -298,6 +304,14 @@ void free_all(jk_opt *o) {
     o->owned.clear();
     for (cudaEvent_t e : o->ev) cudaEventDestroy(e);
     o->ev.clear();
+    for (int i = 0; i < jk_opt::NSIDE; ++i) {
+        if (o->side[i]) cudaStreamDestroy(o->side[i]);
+        if (o->join_ev[i]) cudaEventDestroy(o->join_ev[i]);
+        o->side[i] = nullptr;
+        o->join_ev[i] = nullptr;
+    }
+    if (o->fork_ev) cudaEventDestroy(o->fork_ev);
+    o->fork_ev = nullptr;
 }
 
 __global__ void probe_fma_kernel(double *out, int iters, int fp32) {
@@ -481,6 +495,11 @@ int jk_opt_create(const int32_t *atm, int natm, const int32_t *bas, int nbas, co
     CK(cudaGetDevice(&o->device));
     CK(cudaDeviceGetAttribute(&o->sm_count, cudaDevAttrMultiProcessorCount, o->device));
     if (int e = set_smem_attrs()) return bail(e);
+    CK(cudaEventCreateWithFlags(&o->fork_ev, cudaEventDisableTiming));
+    for (int i = 0; i < jk_opt::NSIDE; ++i) {
+        CK(cudaStreamCreateWithFlags(&o->side[i], cudaStreamNonBlocking));
+        CK(cudaEventCreateWithFlags(&o->join_ev[i], cudaEventDisableTiming));
+    }
     o->nbas = nbas;
     o->tol = tol;
     int ao = 0, prev_l = -1;
@@ -762,7 +781,17 @@ int jk_build(jk_opt *o, const double *dm, int n_dm, int nao, int hermi, int with
             o->ev.push_back(e);
         }
     }
-    for (int q : o->plan_classes) {
+    // Class kernels are independent (they only add into the accumulators), so
+    // unless per-class timing is on they run concurrently on the side
+    // streams, heaviest (highest angular momentum) classes first.
+    const bool concurrent = !o->time_classes;
+    if (concurrent) {
+        CK(cudaEventRecord(o->fork_ev, st));
+        for (int i = 0; i < jk_opt::NSIDE; ++i) CK(cudaStreamWaitEvent(o->side[i], o->fork_ev, 0));
+    }
+    int nlaunched = 0;
+    for (auto it = o->plan_classes.rbegin(); it != o->plan_classes.rend(); ++it) {
+        const int q = *it;
         const ClassEntry &e = g_tab[q];
         int a = 0;
         while ((a + 1) * (a + 2) / 2 <= q) ++a;
@@ -776,12 +805,13 @@ int jk_build(jk_opt *o, const double *dm, int n_dm, int nao, int hermi, int with
         c.nx = o->npairs[a] * o->nbk[b];
         long long upper = (long long)o->npairs[a] * ((o->npairs[b] + e.qb64 - 1) / e.qb64 + o->nbk[b]);
         if (!d.with_j && !d.with_k) break;
+        cudaStream_t ls = concurrent ? o->side[nlaunched++ % jk_opt::NSIDE] : st;
         c.class_id = q;
         d.counters = want_stats ? o->counters : nullptr;
         c.work = o->work + 2 * q;
         c.q_off = o->off64[q]; c.ket_begin = o->kb64[q]; c.ket_end = o->ke64[q];
         if (o->time_classes) { o->ev_slot.push_back(2 * q); CK(cudaEventRecord(o->ev[2 * (o->ev_slot.size() - 1)], st)); }
-        if (int er = launch_class(e.k64, grid_for(o, upper, e.lean), e.smem64, d, c, 0, st, e.threads64)) return er;
+        if (int er = launch_class(e.k64, grid_for(o, upper, e.lean), e.smem64, d, c, 0, ls, e.threads64)) return er;
         if (o->time_classes) CK(cudaEventRecord(o->ev[2 * (o->ev_slot.size() - 1) + 1], st));
         ++launches;
         if (mixed) {
@@ -790,9 +820,16 @@ int jk_build(jk_opt *o, const double *dm, int n_dm, int nao, int hermi, int with
             c.q_off = o->off32[q]; c.ket_begin = o->kb32[q]; c.ket_end = o->ke32[q];
             long long up32 = (long long)o->npairs[a] * ((o->npairs[b] + e.qb32 - 1) / e.qb32 + o->nbk[b]);
             if (o->time_classes) { o->ev_slot.push_back(2 * q + 1); CK(cudaEventRecord(o->ev[2 * (o->ev_slot.size() - 1)], st)); }
-            if (int er = launch_class(e.k32, grid_for(o, up32, e.lean), e.smem32, d, c, 0, st, e.threads32)) return er;
+            cudaStream_t ls32 = concurrent ? o->side[nlaunched++ % jk_opt::NSIDE] : st;
+            if (int er = launch_class(e.k32, grid_for(o, up32, e.lean), e.smem32, d, c, 0, ls32, e.threads32)) return er;
             if (o->time_classes) CK(cudaEventRecord(o->ev[2 * (o->ev_slot.size() - 1) + 1], st));
             ++launches;
+        }
+    }
+    if (concurrent) {
+        for (int i = 0; i < jk_opt::NSIDE; ++i) {
+            CK(cudaEventRecord(o->join_ev[i], o->side[i]));
+            CK(cudaStreamWaitEvent(st, o->join_ev[i], 0));
         }
     }
     {
