@@ -237,25 +237,39 @@ def run_gpu(args):
     # reference results for the error of the mixed build
     vj64, vk64 = opt._build(dms, 1, True, True)
 
-    # mixed precision build
-    opt.precision, opt.split_thresh = 'mixed', args.split
-    opt._build(dms, 1, True, True, stats=True)
-    stmix = dict(opt.last_stats)
-    buildmx = lambda: opt._build(dms, 1, True, True)
-    for _ in range(args.warmup):
-        buildmx()
-    tmx = timed(buildmx, args.steps)
-    vjm, vkm = opt._build(dms, 1, True, True)
+    # mixed precision builds: the configured split, then a sweep
     dmc = dms[0]
-    de = float((0.5 * torch.sum(dmc * (vjm[0] - vj64[0])) - 0.25 * torch.sum(dmc * (vkm[0] - vk64[0]))).item())
-    mixed = {'split': args.split, 'value': (stmix['quartets_fp64'] + stmix['quartets_fp32']) / (sum(tmx) / args.steps),
-             'unit': 'quartets/s', 's_per_jk_build': sum(tmx) / args.steps,
-             'speedup_vs_fp64': (sum(t64) / args.steps) / (sum(tmx) / args.steps),
-             'quartets_fp32': stmix['quartets_fp32'], 'quartets_fp64': stmix['quartets_fp64'],
-             'max_abs_dJ_sorted': float(abs(vjm - vj64).max().item()),
-             'max_abs_dK_sorted': float(abs(vkm - vk64).max().item()),
-             'dE_2e_Ha': de}
-    opt.precision = 'fp64'
+    t64s = sum(t64) / args.steps
+
+    def mixed_eval(split, prec, steps):
+        opt.precision, opt.split_thresh = prec, split
+        opt._build(dms, 1, True, True, stats=True)
+        st = dict(opt.last_stats)
+        fn = lambda: opt._build(dms, 1, True, True)
+        for _ in range(2):
+            fn()
+        tm = sum(timed(fn, steps)) / steps
+        vjm, vkm = opt._build(dms, 1, True, True)
+        de = float((0.5 * torch.sum(dmc * (vjm[0] - vj64[0]))
+                    - 0.25 * torch.sum(dmc * (vkm[0] - vk64[0]))).item())
+        opt.precision = 'fp64'
+        return {'split': split, 'precision': prec,
+                'value': (st['quartets_fp64'] + st['quartets_fp32']) / tm, 'unit': 'quartets/s',
+                's_per_jk_build': tm, 'speedup_vs_fp64': t64s / tm,
+                'quartets_fp32': st['quartets_fp32'], 'quartets_fp64': st['quartets_fp64'],
+                'max_abs_dJ_sorted': float(abs(vjm - vj64).max().item()),
+                'max_abs_dK_sorted': float(abs(vkm - vk64).max().item()),
+                'dE_2e_Ha': de}
+
+    mixed = mixed_eval(args.split, 'mixed', args.steps)
+    sweep = []
+    for split in (1e-8, 1e-6, 1e-4, 1e-3, 1e-2):
+        for prec in ('mixed', 'mixed-fp32roots'):
+            r = mixed_eval(split, prec, 2)
+            sweep.append([split, prec, round(r['s_per_jk_build'], 5), round(r['speedup_vs_fp64'], 3),
+                          r['max_abs_dJ_sorted'], r['max_abs_dK_sorted'], r['dE_2e_Ha']])
+    mixed['sweep'] = {'columns': ['split', 'precision', 's_per_jk_build', 'speedup_vs_fp64',
+                                  'max_abs_dJ', 'max_abs_dK', 'dE_2e_Ha'], 'rows': sweep}
 
     # per-class kernel times (CUDA events on the build stream) for the roofline
     h = opt._handle

@@ -65,6 +65,7 @@ struct EngineDev {
     int nbas, nao, n_dm, n_dmk;
     int with_j, with_k;
     float log_cut;
+    int fp32_asym;            // 1: FP32 quartets take the large-T asymptote in FP32 too
 };
 
 // Work of one quartet class.  The ket list is split into buckets of equal

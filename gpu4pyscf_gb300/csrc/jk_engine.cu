@@ -733,11 +733,12 @@ int jk_build(jk_opt *o, const double *dm, int n_dm, int nao, int hermi, int with
     if (!o || !dm || n_dm <= 0 || nao != o->nao || hermi < 0 || hermi > 2 || (!with_j && !with_k))
         return fail(JK_ERR_ARG, "jk_build: invalid arguments");
     if ((with_j && !vj) || (with_k && !vk)) return fail(JK_ERR_ARG, "jk_build: missing output buffer");
-    if (precision != JK_PREC_FP64 && precision != JK_PREC_MIXED) return fail(JK_ERR_ARG, "jk_build: bad precision");
-    if (precision == JK_PREC_MIXED && !(split_thresh > 0)) return fail(JK_ERR_ARG, "jk_build: split_thresh must be > 0");
+    if (precision != JK_PREC_FP64 && precision != JK_PREC_MIXED && precision != JK_PREC_MIXED_FP32ROOTS)
+        return fail(JK_ERR_ARG, "jk_build: bad precision");
+    if (precision != JK_PREC_FP64 && !(split_thresh > 0)) return fail(JK_ERR_ARG, "jk_build: split_thresh must be > 0");
     cudaStream_t st = (cudaStream_t)stream;
     if (int e = ensure_workspace(o, n_dm)) return e;
-    const int mixed = precision == JK_PREC_MIXED;
+    const int mixed = precision != JK_PREC_FP64;
     const size_t nn = (size_t)nao * nao;
     const int n_dmk = hermi == 0 ? 2 * n_dm : n_dm;
     int launches = 0;
@@ -772,6 +773,7 @@ int jk_build(jk_opt *o, const double *dm, int n_dm, int nao, int hermi, int with
     d.with_j = with_j && hermi != 2;
     d.with_k = with_k;
     d.log_cut = o->tol > 0 ? (float)std::log(o->tol) : -1e30f;
+    d.fp32_asym = precision == JK_PREC_MIXED_FP32ROOTS;
     o->ev_slot.clear();
     if (o->time_classes) {
         size_t need = 4 * o->plan_classes.size();

@@ -246,7 +246,7 @@ rys_class_kernel(EngineDev d, ClassDev c, int ntiles_static)
                     float T = p * q * ipq * (PQx * PQx + PQy * PQy + PQz * PQz);
                     float pref = (float)TWO_PI25 * b1.w * b2.w * ip1 * ip2 * rs;
                     float u[NR], w[NR];
-                    rys_roots_f<NR>(T, d.rys_coef_f, u, w);
+                    rys_roots_f<NR>(T, d.rys_coef_f, u, w, d.fp32_asym);
 #pragma unroll
                     for (int r = 0; r < NR; ++r) { myrw[r] = (Real)u[r]; myrw[NR + r] = (Real)(w[r] * pref); }
                     m[0] = (Real)(0.5f * ip1); m[1] = (Real)(0.5f * ip2);

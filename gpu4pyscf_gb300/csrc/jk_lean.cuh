@@ -233,7 +233,7 @@ rys_lean_kernel(EngineDev d, ClassDev c, int unused)
                 } else {
                     rs = rsqrtf(p + q);
                     float T = p * q * rs * rs * (PQx * PQx + PQy * PQy + PQz * PQz);
-                    rys_roots_f<NR>(T, d.rys_coef_f, u, w);
+                    rys_roots_f<NR>(T, d.rys_coef_f, u, w, d.fp32_asym);
                 }
                 const Real ipq = rs * rs;
                 const Real pref = Real(34.98683665524972497) * Kb * Kk * ipb * ipk * rs;

@@ -52,10 +52,24 @@ __device__ __forceinline__ void rys_roots(double T, const double *__restrict__ c
     for (int r = 0; r < NR; ++r) { u[r] = a[r]; w[r] = a[NR + r]; }
 }
 
-// FP32 roots: table in float; the asymptote in FP64
+// FP32 roots: table in float; the asymptote in FP64 (or in FP32 when
+// asym32 is set: u = h^2/T, w = W/sqrt(T) have no cancellation, so FP32
+// keeps its relative 1e-7 there)
 template <int NR>
-__device__ __forceinline__ void rys_roots_f(float T, const float *__restrict__ coef, float *u, float *w) {
+__device__ __forceinline__ void rys_roots_f(float T, const float *__restrict__ coef, float *u, float *w,
+                                            int asym32 = 0) {
     if (!(T < 2.f * rys_nint(NR))) {
+        if (asym32) {
+            const float rs = rsqrtf(T);
+            const float it = rs * rs;
+            constexpr int o = NR * (NR - 1) / 2;
+#pragma unroll
+            for (int r = 0; r < NR; ++r) {
+                u[r] = (float)c_rys_asym_x2[o + r] * it;
+                w[r] = (float)c_rys_asym_w[o + r] * rs;
+            }
+            return;
+        }
         double ud[NR], wd[NR];
         rys_asym<NR>((double)T, ud, wd);
 #pragma unroll

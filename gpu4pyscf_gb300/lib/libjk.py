@@ -13,6 +13,7 @@ LIB_PATH = os.path.join(_HERE, 'libgb300jk.so')
 
 JK_PREC_FP64 = 0
 JK_PREC_MIXED = 1
+JK_PREC_MIXED_FP32ROOTS = 2
 
 
 class JKStats(ctypes.Structure):

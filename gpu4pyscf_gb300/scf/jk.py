@@ -9,8 +9,8 @@ sm_103a kernels of libgb300jk.so; there is no CPU path.
 
 Differences from the reference, by design:
 * device arrays are torch CUDA tensors (the reference uses CuPy);
-* ``_VHFOpt.precision`` ('fp64' or 'mixed') and ``_VHFOpt.split_thresh``
-  select the mixed FP32/FP64 evaluation;
+* ``_VHFOpt.precision`` ('fp64', 'mixed' or 'mixed-fp32roots') and
+  ``_VHFOpt.split_thresh`` select the mixed FP32/FP64 evaluation;
 * range-separated operators (omega != 0) are not implemented and raise.
 """
 
@@ -140,7 +140,8 @@ class _VHFOpt:
         n_dm, nao = dms.shape[0], dms.shape[-1]
         vj = torch.empty_like(dms) if with_j else None
         vk = torch.empty_like(dms) if with_k else None
-        prec = libjk.JK_PREC_MIXED if self.precision == 'mixed' else libjk.JK_PREC_FP64
+        prec = {'fp64': libjk.JK_PREC_FP64, 'mixed': libjk.JK_PREC_MIXED,
+                'mixed-fp32roots': libjk.JK_PREC_MIXED_FP32ROOTS}[self.precision]
         st = libjk.JKStats() if stats else None
         stream = torch.cuda.current_stream().cuda_stream
         err = libjk.load().jk_build(self._handle, dms.data_ptr(), n_dm, nao, int(hermi),

@@ -32,7 +32,9 @@ typedef struct jk_opt jk_opt;
 
 /* Precision modes of jk_build */
 #define JK_PREC_FP64 0   /* every quartet in FP64 */
-#define JK_PREC_MIXED 1  /* quartets whose bound < split_thresh in FP32, FP64 accumulation */
+#define JK_PREC_MIXED 1  /* quartets whose bound < split_thresh in FP32, FP64 accumulation;
+                            large-T Rys roots of those quartets in FP64 */
+#define JK_PREC_MIXED_FP32ROOTS 2  /* as JK_PREC_MIXED, large-T roots in FP32 as well */
 
 /* Error codes */
 #define JK_OK 0
@@ -79,8 +81,8 @@ int jk_opt_get_qcond(const jk_opt *opt, double *q);
  * hermi: 0 general, 1 symmetric, 2 antisymmetric (vj set to zero).
  * vj, vk: device [n_dm][nao][nao] float64 outputs (either may be NULL when
  *         with_j / with_k is 0).
- * precision: JK_PREC_FP64 or JK_PREC_MIXED with split_thresh the bound below
- *            which a quartet is evaluated in FP32.
+ * precision: JK_PREC_FP64, JK_PREC_MIXED or JK_PREC_MIXED_FP32ROOTS with
+ *            split_thresh the bound below which a quartet is evaluated in FP32.
  * stream: cudaStream_t of the caller (NULL = legacy default stream).
  * stats: optional host output. */
 int jk_build(jk_opt *opt, const double *dm, int n_dm, int nao, int hermi,
