@@ -31,7 +31,9 @@ struct __align__(32) d4 { double x, y, z, w; };
 
 struct ShellDev {
     double x, y, z;
-    int l, nprim, ao, pad;
+    int l, nprim;
+    int ao;    // first Cartesian AO within the shell's molecule
+    int mol;   // molecule of the shell (0 for a single molecule)
 };
 
 // one pair class (li, lj) with pairs sorted by Schwarz factor, descending
@@ -63,6 +65,12 @@ struct EngineDev {
     float *qout;              // Schwarz mode output (per pair)
     unsigned long long *counters;  // per class: [quartets, prim quartets]
     int nbas, nao, n_dm, n_dmk;
+    // densities and J/K are stored per molecule as packed square blocks:
+    // element (a, b) of molecule m in density idm sits at
+    // idm * ntot + mol_base[m] + a * mol_nao[m] + b
+    long long ntot;
+    const long long *mol_base;
+    const int *mol_nao;
     int with_j, with_k;
     float log_cut;
     int fp32_asym;            // 1: FP32 quartets take the large-T asymptote in FP32 too

@@ -86,14 +86,34 @@ inline int ncart_h(int l) { return (l + 1) * (l + 2) / 2; }
 // small device kernels: densities, screening table, planning, epilogue
 // ---------------------------------------------------------------------------
 
-__global__ void prep_dm_kernel(const double *dm, int n_dm, int nao, int hermi, int mixed,
+// Packed block layout of densities and J/K: one square block per molecule.
+struct Layout {
+    int nmol;
+    long long ntot;              // elements per density
+    const long long *mol_base;   // [nmol] first element of each block
+    const int *mol_nao;          // [nmol] block size
+};
+
+// element r of a density -> index of the transposed element
+__device__ __forceinline__ size_t transposed(const Layout &L, size_t r) {
+    int lo = 0, hi = L.nmol;
+    while (hi - lo > 1) {
+        int mid = (lo + hi) >> 1;
+        if ((size_t)__ldg(L.mol_base + mid) <= r) lo = mid; else hi = mid;
+    }
+    const size_t base = (size_t)__ldg(L.mol_base + lo);
+    const size_t n = (size_t)__ldg(L.mol_nao + lo);
+    const size_t t = r - base;
+    return base + (t % n) * n + t / n;
+}
+
+__global__ void prep_dm_kernel(const double *dm, int n_dm, Layout L, int hermi, int mixed,
                                double *dmj, double *dmk, float *dmj_f, float *dmk_f) {
-    size_t nn = (size_t)nao * nao;
-    size_t total = nn * n_dm;
+    const size_t nn = (size_t)L.ntot;
+    const size_t total = nn * n_dm;
     for (size_t x = blockIdx.x * (size_t)blockDim.x + threadIdx.x; x < total; x += (size_t)gridDim.x * blockDim.x) {
         size_t idm = x / nn, r = x % nn;
-        size_t i = r / nao, j = r % nao;
-        double a = dm[x], at = dm[idm * nn + j * nao + i];
+        double a = dm[x], at = dm[idm * nn + transposed(L, r)];
         double js = a + at;
         dmj[x] = js;
         dmk[x] = a;
@@ -106,19 +126,24 @@ __global__ void prep_dm_kernel(const double *dm, int n_dm, int nao, int hermi, i
     }
 }
 
-__global__ void dm_cond_kernel(const double *dm, int n_dm, int nao, const ShellDev *sh, int nbas,
+// per shell pair: log of the largest |D| over its block in every density
+// (symmetrised for hermi=0); shells of different molecules get -690
+__global__ void dm_cond_kernel(const double *dm, int n_dm, Layout L, const ShellDev *sh, int nbas,
                                int hermi, float *dm_cond) {
     int ij = blockIdx.x * blockDim.x + threadIdx.x;
     if (ij >= nbas * nbas) return;
     int i = ij / nbas, j = ij % nbas;
+    if (sh[i].mol != sh[j].mol) { dm_cond[ij] = -690.f; return; }
+    const size_t base = (size_t)L.mol_base[sh[i].mol];
+    const size_t nao = (size_t)L.mol_nao[sh[i].mol];
     int ni = (sh[i].l + 1) * (sh[i].l + 2) / 2, nj = (sh[j].l + 1) * (sh[j].l + 2) / 2;
-    size_t nn = (size_t)nao * nao;
+    const size_t nn = (size_t)L.ntot;
     double mij = 0., mji = 0.;
     for (int d = 0; d < n_dm; ++d)
         for (int a = 0; a < ni; ++a)
             for (int b = 0; b < nj; ++b) {
-                mij = fmax(mij, fabs(dm[d * nn + (size_t)(sh[i].ao + a) * nao + sh[j].ao + b]));
-                mji = fmax(mji, fabs(dm[d * nn + (size_t)(sh[j].ao + b) * nao + sh[i].ao + a]));
+                mij = fmax(mij, fabs(dm[d * nn + base + (size_t)(sh[i].ao + a) * nao + sh[j].ao + b]));
+                mji = fmax(mji, fabs(dm[d * nn + base + (size_t)(sh[j].ao + b) * nao + sh[i].ao + a]));
             }
     double v = hermi == 0 ? mij + mji : fmax(mij, mji);
     dm_cond[ij] = (float)log(v + 1e-300);
@@ -140,7 +165,11 @@ __global__ void max_kernel(const float *x, int n, float *out) {
 struct PlanClass {
     const float *bra_logq;
     const float *ket_logq;
-    const int *ket_bstart;  // [nbk + 1] bucket boundaries of the ket list
+    const int *ket_bstart;  // bucket boundaries of the ket list
+    const int *ket_mb0;     // [nmol] first ket bucket of each molecule
+    const int *ket_mbn;     // [nmol] ket buckets of each molecule
+    const int2 *bra_ij;
+    const ShellDev *shells;
     int nbra, nket, nbk, same, qb64, qb32;
     int *kb64, *ke64, *cnt64, *kb32, *ke32, *cnt32;  // [nbra * nbk]
     int start;  // offset in the flattened (class, bra, bucket) index space
@@ -171,7 +200,15 @@ __global__ void plan_kernel(const PlanClass *pcs, int npc, int total, const floa
     const PlanClass &p = pcs[lo];
     int x = g - p.start;
     if (x >= p.nbra * p.nbk) return;
-    int ib = x % p.nbra, k = x / p.nbra;  // ket-bucket major
+    int ib = x % p.nbra, kl = x / p.nbra;  // ket-bucket major
+    // kets of the bra's molecule only: kl-th bucket of that molecule
+    const int mol = p.shells[p.bra_ij[ib].x].mol;
+    if (kl >= p.ket_mbn[mol]) {
+        p.kb64[x] = p.ke64[x] = p.kb32[x] = p.ke32[x] = 0;
+        p.cnt64[x] = p.cnt32[x] = 0;
+        return;
+    }
+    const int k = p.ket_mb0[mol] + kl;
     int b0 = p.ket_bstart[k], b1 = p.ket_bstart[k + 1];
     float base = p.bra_logq[ib] + dm_max[0];
     int end = b0 + count_ge(p.ket_logq + b0, b1 - b0, log_cut - base);
@@ -217,19 +254,18 @@ __global__ void scan_kernel(const ScanJob *jobs) {
     if (threadIdx.x == 0) jb.off[jb.n] = carry;
 }
 
-__global__ void epilogue_kernel(const double *jt, const double *kt, int n_dm, int nao, int hermi,
+__global__ void epilogue_kernel(const double *jt, const double *kt, int n_dm, Layout L, int hermi,
                                 int with_j, int with_k, double *vj, double *vk) {
-    size_t nn = (size_t)nao * nao;
-    size_t total = nn * n_dm;
+    const size_t nn = (size_t)L.ntot;
+    const size_t total = nn * n_dm;
     for (size_t x = blockIdx.x * (size_t)blockDim.x + threadIdx.x; x < total; x += (size_t)gridDim.x * blockDim.x) {
         size_t idm = x / nn, r = x % nn;
-        size_t i = r / nao, j = r % nao;
-        size_t xt = idm * nn + j * nao + i;
+        size_t xt = idm * nn + transposed(L, r);
         if (with_j) vj[x] = hermi == 2 ? 0. : jt[x] + jt[xt];
         if (with_k) {
             if (hermi == 1) vk[x] = kt[x] + kt[xt];
             else if (hermi == 2) vk[x] = kt[x] - kt[xt];
-            else vk[x] = kt[x] + kt[(n_dm + idm) * nn + j * nao + i];
+            else vk[x] = kt[x] + kt[n_dm * nn + xt];
         }
     }
 }
@@ -266,8 +302,17 @@ struct jk_opt {
     int2 *pl_ij[NPAIRCLASS] = {nullptr};
     float *pl_logq[NPAIRCLASS] = {nullptr};
     int *pl_prim[NPAIRCLASS] = {nullptr};
-    int nbk[NPAIRCLASS] = {0};           // primitive-count buckets per pair class
-    int *pl_bstart[NPAIRCLASS] = {nullptr};
+    int nbk[NPAIRCLASS] = {0};           // ket buckets per molecule (max over molecules)
+    int *pl_bstart[NPAIRCLASS] = {nullptr};  // bucket boundaries (molecule, primitive count)
+    int *pl_mb0[NPAIRCLASS] = {nullptr};     // [nmol] first bucket of each molecule
+    int *pl_mbn[NPAIRCLASS] = {nullptr};     // [nmol] buckets of each molecule
+    // molecules: packed block layout of densities and J/K
+    int nmol = 1;
+    long long ntot = 0;
+    std::vector<long long> mol_base_h;
+    std::vector<int> mol_nao_h;
+    long long *mol_base = nullptr;
+    int *mol_nao = nullptr;
     std::vector<double> qcond_h;  // [nbas*nbas]
     // planning buffers per quartet class
     int *kb64[NQCLASS] = {nullptr}, *ke64[NQCLASS] = {nullptr}, *cnt64[NQCLASS] = {nullptr}, *off64[NQCLASS] = {nullptr};
@@ -397,7 +442,12 @@ EngineDev base_engine(const jk_opt *o) {
     d.pp_af = o->pp_af; d.pp_bf = o->pp_bf; d.pp_ipf = o->pp_ipf;
     d.rys_coef = o->rys_coef; d.rys_coef_f = o->rys_coef_f;
     d.nbas = o->nbas; d.nao = o->nao;
+    d.ntot = o->ntot; d.mol_base = o->mol_base; d.mol_nao = o->mol_nao;
     return d;
+}
+
+Layout layout_of(const jk_opt *o) {
+    return Layout{o->nmol, o->ntot, o->mol_base, o->mol_nao};
 }
 
 int grid_for(const jk_opt *o, long long upper_tiles, int lean = 0) {
@@ -483,10 +533,12 @@ void jk_opt_destroy(jk_opt *opt) {
     delete opt;
 }
 
-int jk_opt_create(const int32_t *atm, int natm, const int32_t *bas, int nbas, const double *env, int nenv,
-                  double tol, int flags, jk_opt **out) {
-    (void)flags;
-    if (!atm || !bas || !env || !out || natm <= 0 || nbas <= 0 || nenv <= 0 || !(tol >= 0))
+// shell_mol / shell_ao / mol_nao: molecule of each shell, its first AO
+// within the molecule, AOs per molecule (all null for one molecule).
+static int create_impl(const int32_t *atm, int natm, const int32_t *bas, int nbas, const double *env, int nenv,
+                       const int32_t *shell_mol, const int32_t *shell_ao, int nmol, const int32_t *mol_nao,
+                       double tol, jk_opt **out) {
+    if (!atm || !bas || !env || !out || natm <= 0 || nbas <= 0 || nenv <= 0 || !(tol >= 0) || nmol <= 0)
         return fail(JK_ERR_ARG, "jk_opt_create: invalid arguments");
     std::call_once(g_tab_once, init_registry);
     jk_opt *o = new jk_opt();
@@ -519,7 +571,13 @@ int jk_opt_create(const int32_t *atm, int natm, const int32_t *bas, int nbas, co
         s.x = env[pcoord]; s.y = env[pcoord + 1]; s.z = env[pcoord + 2];
         if (!std::isfinite(s.x) || !std::isfinite(s.y) || !std::isfinite(s.z))
             return bail(fail(JK_ERR_ARG, "non-finite coordinates"));
-        s.l = l; s.nprim = np; s.ao = ao; s.pad = 0;
+        s.l = l; s.nprim = np; s.ao = ao; s.mol = 0;
+        if (shell_mol) {
+            s.mol = shell_mol[i];
+            s.ao = shell_ao[i];
+            if (s.mol < 0 || s.mol >= nmol || s.ao < 0 || s.ao + ncart_h(l) > mol_nao[s.mol])
+                return bail(fail(JK_ERR_ARG, "shell molecule or AO offset out of range"));
+        }
         ao += ncart_h(l);
         o->prim0_h.push_back((int)o->exps_h.size());
         for (int p = 0; p < np; ++p) {
@@ -530,7 +588,18 @@ int jk_opt_create(const int32_t *atm, int natm, const int32_t *bas, int nbas, co
         }
         o->shells_h.push_back(s);
     }
-    o->nao = ao;
+    o->nao = shell_mol ? 0 : ao;
+    o->nmol = nmol;
+    o->ntot = 0;
+    for (int m = 0; m < nmol; ++m) {
+        int n = shell_mol ? mol_nao[m] : ao;
+        if (n <= 0) return bail(fail(JK_ERR_ARG, "molecule without AOs"));
+        o->mol_base_h.push_back(o->ntot);
+        o->mol_nao_h.push_back(n);
+        o->ntot += (long long)n * n;
+    }
+    if (int e = own_upload(o, &o->mol_base, o->mol_base_h)) return bail(e);
+    if (int e = own_upload(o, &o->mol_nao, o->mol_nao_h)) return bail(e);
     if (int e = own_upload(o, &o->shells, o->shells_h)) return bail(e);
     {
         std::vector<double> t(rys_coef_host, rys_coef_host + RYS_TABLE_SIZE);
@@ -546,6 +615,7 @@ int jk_opt_create(const int32_t *atm, int natm, const int32_t *bas, int nbas, co
     for (int i = 0; i < nbas; ++i)
         for (int j = 0; j <= i; ++j) {
             const ShellDev &A = o->shells_h[i], &B = o->shells_h[j];
+            if (A.mol != B.mol) continue;
             double AB2 = (A.x - B.x) * (A.x - B.x) + (A.y - B.y) * (A.y - B.y) + (A.z - B.z) * (A.z - B.z);
             double best = 1e300;
             for (int pa = 0; pa < A.nprim; ++pa)
@@ -623,18 +693,36 @@ int jk_opt_create(const int32_t *atm, int natm, const int32_t *bas, int nbas, co
                 const int2 &p = cand[pc].ij[k];
                 return o->shells_h[p.x].nprim * o->shells_h[p.y].nprim;
             };
+            auto molp = [&](int k) { return o->shells_h[cand[pc].ij[k].x].mol; };
+            // order: molecule, primitive count (descending), Schwarz factor (descending)
             std::stable_sort(idx.begin(), idx.end(), [&](int a, int b) {
+                int ma = molp(a), mb = molp(b);
+                if (ma != mb) return ma < mb;
                 int na = npp(a), nb = npp(b);
                 if (na != nb) return na > nb;
                 return qh[pc][a] > qh[pc][b];
             });
-            std::vector<int> bstart{0};
-            for (size_t t = 1; t < idx.size(); ++t)
-                if (npp(idx[t]) != npp(idx[t - 1])) bstart.push_back((int)t);
+            // buckets: runs of equal (molecule, primitive count)
+            std::vector<int> bstart{0}, bmol;
+            for (size_t t = 0; t < idx.size(); ++t) {
+                if (t > 0 && (npp(idx[t]) != npp(idx[t - 1]) || molp(idx[t]) != molp(idx[t - 1])))
+                    bstart.push_back((int)t);
+                if (bmol.size() < bstart.size()) bmol.push_back(molp(idx[t]));
+            }
             bstart.push_back((int)idx.size());
-            if (idx.empty()) bstart = {0, 0};
-            o->nbk[pc] = (int)bstart.size() - 1;
+            if (idx.empty()) { bstart = {0, 0}; bmol = {0}; }
+            std::vector<int> mb0(nmol, 0), mbn(nmol, 0);
+            for (int k = (int)bmol.size() - 1; k >= 0; --k) {
+                if (idx.empty()) break;
+                mb0[bmol[k]] = k;
+                mbn[bmol[k]] += 1;
+            }
+            int maxb = 0;
+            for (int m = 0; m < nmol; ++m) maxb = std::max(maxb, mbn[m]);
+            o->nbk[pc] = std::max(maxb, 1);
             if (int e = own_upload(o, &o->pl_bstart[pc], bstart)) return bail(e);
+            if (int e = own_upload(o, &o->pl_mb0[pc], mb0)) return bail(e);
+            if (int e = own_upload(o, &o->pl_mbn[pc], mbn)) return bail(e);
             HostPairList fin;
             for (int k : idx) {
                 const int2 &p = cand[pc].ij[k];
@@ -685,6 +773,10 @@ int jk_opt_create(const int32_t *atm, int natm, const int32_t *bas, int nbas, co
             p.bra_logq = o->pl_logq[a];
             p.ket_logq = o->pl_logq[b];
             p.ket_bstart = o->pl_bstart[b];
+            p.ket_mb0 = o->pl_mb0[b];
+            p.ket_mbn = o->pl_mbn[b];
+            p.bra_ij = o->pl_ij[a];
+            p.shells = o->shells;
             p.nbra = nb; p.nket = nk; p.nbk = o->nbk[b]; p.same = (a == b);
             p.qb64 = e.qb64; p.qb32 = e.qb32;
             p.kb64 = o->kb64[q]; p.ke64 = o->ke64[q]; p.cnt64 = o->cnt64[q];
@@ -709,6 +801,20 @@ int jk_opt_create(const int32_t *atm, int natm, const int32_t *bas, int nbas, co
     return 0;
 }
 
+int jk_opt_create(const int32_t *atm, int natm, const int32_t *bas, int nbas, const double *env, int nenv,
+                  double tol, int flags, jk_opt **out) {
+    (void)flags;
+    return create_impl(atm, natm, bas, nbas, env, nenv, nullptr, nullptr, 1, nullptr, tol, out);
+}
+
+int jk_opt_create_batch(const int32_t *atm, int natm, const int32_t *bas, int nbas, const double *env, int nenv,
+                        const int32_t *shell_mol, const int32_t *shell_ao, int nmol, const int32_t *mol_nao,
+                        double tol, int flags, jk_opt **out) {
+    (void)flags;
+    if (!shell_mol || !shell_ao || !mol_nao) return fail(JK_ERR_ARG, "jk_opt_create_batch: null molecule arrays");
+    return create_impl(atm, natm, bas, nbas, env, nenv, shell_mol, shell_ao, nmol, mol_nao, tol, out);
+}
+
 static int ensure_workspace(jk_opt *o, int n_dm) {
     if (n_dm <= o->ws_ndm) return 0;
     for (void *p : {(void *)o->dmj, (void *)o->dmk, (void *)o->jt, (void *)o->kt, (void *)o->dmj_f, (void *)o->dmk_f}) {
@@ -717,7 +823,7 @@ static int ensure_workspace(jk_opt *o, int n_dm) {
         if (it != o->owned.end()) o->owned.erase(it);
         cudaFree(p);
     }
-    size_t nn = (size_t)o->nao * o->nao;
+    size_t nn = (size_t)o->ntot;
     if (int e = own_alloc(o, &o->dmj, nn * n_dm)) return e;
     if (int e = own_alloc(o, &o->dmk, nn * 2 * n_dm)) return e;
     if (int e = own_alloc(o, &o->jt, nn * n_dm)) return e;
@@ -728,9 +834,9 @@ static int ensure_workspace(jk_opt *o, int n_dm) {
     return 0;
 }
 
-int jk_build(jk_opt *o, const double *dm, int n_dm, int nao, int hermi, int with_j, int with_k, int precision,
-             double split_thresh, double *vj, double *vk, void *stream, jk_stats *stats) {
-    if (!o || !dm || n_dm <= 0 || nao != o->nao || hermi < 0 || hermi > 2 || (!with_j && !with_k))
+static int build_impl(jk_opt *o, const double *dm, int n_dm, int hermi, int with_j, int with_k, int precision,
+                      double split_thresh, double *vj, double *vk, void *stream, jk_stats *stats) {
+    if (!o || !dm || n_dm <= 0 || hermi < 0 || hermi > 2 || (!with_j && !with_k))
         return fail(JK_ERR_ARG, "jk_build: invalid arguments");
     if ((with_j && !vj) || (with_k && !vk)) return fail(JK_ERR_ARG, "jk_build: missing output buffer");
     if (precision != JK_PREC_FP64 && precision != JK_PREC_MIXED && precision != JK_PREC_MIXED_FP32ROOTS)
@@ -739,14 +845,15 @@ int jk_build(jk_opt *o, const double *dm, int n_dm, int nao, int hermi, int with
     cudaStream_t st = (cudaStream_t)stream;
     if (int e = ensure_workspace(o, n_dm)) return e;
     const int mixed = precision != JK_PREC_FP64;
-    const size_t nn = (size_t)nao * nao;
+    const size_t nn = (size_t)o->ntot;
+    const Layout L = layout_of(o);
     const int n_dmk = hermi == 0 ? 2 * n_dm : n_dm;
     int launches = 0;
     {
         int grid = (int)std::min<size_t>((nn * n_dm + 255) / 256, (size_t)o->sm_count * 8);
-        prep_dm_kernel<<<grid, 256, 0, st>>>(dm, n_dm, nao, hermi, mixed, o->dmj, o->dmk, o->dmj_f, o->dmk_f);
+        prep_dm_kernel<<<grid, 256, 0, st>>>(dm, n_dm, L, hermi, mixed, o->dmj, o->dmk, o->dmj_f, o->dmk_f);
         int nb2 = o->nbas * o->nbas;
-        dm_cond_kernel<<<(nb2 + 255) / 256, 256, 0, st>>>(dm, n_dm, nao, o->shells, o->nbas, hermi, o->dm_cond);
+        dm_cond_kernel<<<(nb2 + 255) / 256, 256, 0, st>>>(dm, n_dm, L, o->shells, o->nbas, hermi, o->dm_cond);
         max_kernel<<<1, 1024, 0, st>>>(o->dm_cond, nb2, o->dm_max);
         launches += 3;
     }
@@ -836,7 +943,7 @@ int jk_build(jk_opt *o, const double *dm, int n_dm, int nao, int hermi, int with
     }
     {
         int grid = (int)std::min<size_t>((nn * n_dm + 255) / 256, (size_t)o->sm_count * 8);
-        epilogue_kernel<<<grid, 256, 0, st>>>(o->jt, o->kt, n_dm, nao, hermi, with_j, with_k, vj, vk);
+        epilogue_kernel<<<grid, 256, 0, st>>>(o->jt, o->kt, n_dm, L, hermi, with_j, with_k, vj, vk);
         ++launches;
     }
     CK(cudaGetLastError());
@@ -864,6 +971,19 @@ int jk_build(jk_opt *o, const double *dm, int n_dm, int nao, int hermi, int with
     }
     return 0;
 }
+
+int jk_build(jk_opt *o, const double *dm, int n_dm, int nao, int hermi, int with_j, int with_k, int precision,
+             double split_thresh, double *vj, double *vk, void *stream, jk_stats *stats) {
+    if (!o || o->nmol != 1 || nao != o->nao) return fail(JK_ERR_ARG, "jk_build: invalid arguments");
+    return build_impl(o, dm, n_dm, hermi, with_j, with_k, precision, split_thresh, vj, vk, stream, stats);
+}
+
+int jk_build_batch(jk_opt *o, const double *dm, int n_dm, int hermi, int with_j, int with_k, int precision,
+                   double split_thresh, double *vj, double *vk, void *stream, jk_stats *stats) {
+    return build_impl(o, dm, n_dm, hermi, with_j, with_k, precision, split_thresh, vj, vk, stream, stats);
+}
+
+long long jk_opt_ntot(const jk_opt *o) { return o ? o->ntot : -1; }
 
 }  // extern "C"
 
@@ -919,7 +1039,7 @@ extern "C" int jk_noalloc_scratch_bytes(void) { return (int)JK_NOALLOC_SCRATCH_B
 
 extern "C" int jk_build_noalloc(jk_opt *o, const double *dm, int n_dm, int nao, int hermi, int with_j, int with_k,
                                 int precision, double split_thresh, double *vj, double *vk, void *stream) {
-    if (!o || !dm || n_dm <= 0 || nao != o->nao || hermi < 0 || hermi > 2 || (!with_j && !with_k))
+    if (!o || !dm || n_dm <= 0 || o->nmol != 1 || nao != o->nao || hermi < 0 || hermi > 2 || (!with_j && !with_k))
         return fail(JK_ERR_ARG, "jk_build_noalloc: invalid arguments");
     if ((with_j && !vj) || (with_k && !vk)) return fail(JK_ERR_ARG, "jk_build_noalloc: missing output buffer");
     if (precision != JK_PREC_FP64 && precision != JK_PREC_MIXED)
@@ -959,9 +1079,9 @@ extern "C" int jk_build_noalloc(jk_opt *o, const double *dm, int n_dm, int nao, 
     cudaStream_t st = (cudaStream_t)stream;
     {
         int grid = (int)std::min<size_t>((nn * n_dm + 255) / 256, (size_t)o->sm_count * 8);
-        prep_dm_kernel<<<grid, 256, 0, st>>>(dm, n_dm, nao, hermi, mixed, dmj, dmk, dmj_f, dmk_f);
+        prep_dm_kernel<<<grid, 256, 0, st>>>(dm, n_dm, layout_of(o), hermi, mixed, dmj, dmk, dmj_f, dmk_f);
         int nb2 = o->nbas * o->nbas;
-        dm_cond_kernel<<<(nb2 + 255) / 256, 256, 0, st>>>(dm, n_dm, nao, o->shells, o->nbas, hermi, dm_cond);
+        dm_cond_kernel<<<(nb2 + 255) / 256, 256, 0, st>>>(dm, n_dm, layout_of(o), o->shells, o->nbas, hermi, dm_cond);
         max_kernel<<<1, 1024, 0, st>>>(dm_cond, nb2, dm_max);
     }
     if (o->nplan > 0) {
@@ -1014,7 +1134,7 @@ extern "C" int jk_build_noalloc(jk_opt *o, const double *dm, int n_dm, int nao, 
     }
     {
         int grid = (int)std::min<size_t>((nn * n_dm + 255) / 256, (size_t)o->sm_count * 8);
-        epilogue_kernel<<<grid, 256, 0, st>>>(jt, kt, n_dm, nao, hermi, with_j, with_k, vj, vk);
+        epilogue_kernel<<<grid, 256, 0, st>>>(jt, kt, n_dm, layout_of(o), hermi, with_j, with_k, vj, vk);
     }
     CK(cudaGetLastError());
     return 0;

@@ -30,12 +30,12 @@ template <typename Real>
 __device__ __forceinline__ const Real *dm_ptr(const EngineDev &d, bool jpart, int idm);
 template <>
 __device__ __forceinline__ const double *dm_ptr<double>(const EngineDev &d, bool jpart, int idm) {
-    size_t nn = (size_t)d.nao * d.nao;
+    size_t nn = (size_t)d.ntot;
     return jpart ? d.dmj + idm * nn : d.dmk + idm * nn;
 }
 template <>
 __device__ __forceinline__ const float *dm_ptr<float>(const EngineDev &d, bool jpart, int idm) {
-    size_t nn = (size_t)d.nao * d.nao;
+    size_t nn = (size_t)d.ntot;
     return jpart ? d.dmj_f + idm * nn : d.dmk_f + idm * nn;
 }
 
@@ -382,12 +382,14 @@ rys_class_kernel(EngineDev d, ClassDev c, int ntiles_static)
             const int nj = d.with_j ? d.n_dm * NJ : 0;
             const int nk = d.with_k ? d.n_dmk * NK : 0;
             const int per = nj + nk;
-            const int nao = d.nao;
             for (int task = tid; task < QB * per; task += JK_THREADS) {
                 int s = task / per;
                 int t = task % per;
                 const SlotInfo &si = slots[s];
                 if (!si.valid) continue;
+                const int mol = d.shells[si.ish].mol;
+                const int nao = __ldg(d.mol_nao + mol);
+                const size_t mbase = (size_t)__ldg(d.mol_base + mol);
                 const Real *Es = E + s * NF;
                 const int ai = d.shells[si.ish].ao, aj = d.shells[si.jsh].ao;
                 const int ak = d.shells[si.ksh].ao, al = d.shells[si.lsh].ao;
@@ -395,7 +397,7 @@ rys_class_kernel(EngineDev d, ClassDev c, int ntiles_static)
                 double *out;
                 if (t < nj) {
                     int idm = t / NJ, o = t % NJ;
-                    const Real *D = dm_ptr<Real>(d, true, idm);
+                    const Real *D = dm_ptr<Real>(d, true, idm) + mbase;
                     if (o < NFI * NFJ) {
                         int a = o / NFJ, b = o % NFJ;
                         const Real *Er = Es + (a * NFJ + b) * NFK * NFL;
@@ -403,20 +405,20 @@ rys_class_kernel(EngineDev d, ClassDev c, int ntiles_static)
                         for (int cc = 0; cc < NFK; ++cc)
                             for (int dd = 0; dd < NFL; ++dd)
                                 sum += Er[cc * NFL + dd] * D[(size_t)(ak + cc) * nao + al + dd];
-                        out = d.vj + (size_t)idm * nao * nao + (size_t)(ai + a) * nao + aj + b;
+                        out = d.vj + (size_t)idm * d.ntot + mbase + (size_t)(ai + a) * nao + aj + b;
                     } else {
                         o -= NFI * NFJ;
                         int cc = o / NFL, dd = o % NFL;
                         for (int a = 0; a < NFI; ++a)
                             for (int b = 0; b < NFJ; ++b)
                                 sum += Es[(a * NFJ + b) * NFK * NFL + cc * NFL + dd] * D[(size_t)(ai + a) * nao + aj + b];
-                        out = d.vj + (size_t)idm * nao * nao + (size_t)(ak + cc) * nao + al + dd;
+                        out = d.vj + (size_t)idm * d.ntot + mbase + (size_t)(ak + cc) * nao + al + dd;
                     }
                 } else {
                     t -= nj;
                     int idm = t / NK, o = t % NK;
-                    const Real *D = dm_ptr<Real>(d, false, idm);
-                    double *V = d.vk + (size_t)idm * nao * nao;
+                    const Real *D = dm_ptr<Real>(d, false, idm) + mbase;
+                    double *V = d.vk + (size_t)idm * d.ntot + mbase;
                     if (o < NFI * NFK) {            // K[i a, k c] += E[abcd] D[j b, l d]
                         int a = o / NFK, cc = o % NFK;
                         for (int b = 0; b < NFJ; ++b)

@@ -269,16 +269,18 @@ rys_lean_kernel(EngineDev d, ClassDev c, int unused)
             }
         }
         // ---- digestion ----
-        const int nao = d.nao;
-        const size_t nn = (size_t)nao * nao;
+        const int mol = A.mol;
+        const int nao = __ldg(d.mol_nao + mol);
+        const size_t nn = (size_t)d.ntot;
+        const size_t mbase = (size_t)__ldg(d.mol_base + mol);
         const Real fac = Real((pij.x == pij.y ? .5 : 1.) * (pkl.x == pkl.y ? .5 : 1.) *
                               (c.same && ib == ket ? .5 : 1.));
         const int ai = A.ao, aj = B.ao;
         const int ak = valid ? d.shells[pkl.x].ao : 0, al = valid ? d.shells[pkl.y].ao : 0;
         if (d.with_j) {
             for (int idm = 0; idm < d.n_dm; ++idm) {
-                const Real *Dm = LeanIO<Real>::dj(d) + idm * nn;
-                double *V = d.vj + idm * nn;
+                const Real *Dm = LeanIO<Real>::dj(d) + idm * nn + mbase;
+                double *V = d.vj + idm * nn + mbase;
                 Real dkl[NFK * NFL], dij[NFI * NFJ];
 #pragma unroll
                 for (int cc = 0; cc < NFK; ++cc)
@@ -320,8 +322,8 @@ rys_lean_kernel(EngineDev d, ClassDev c, int unused)
             // lanes whose kets share a shell hit the same K elements: add
             // through warp aggregation (idle lanes contribute nothing)
             for (int idm = 0; idm < d.n_dmk; ++idm) {
-                const Real *Dm = LeanIO<Real>::dk(d) + idm * nn;
-                double *V = d.vk + idm * nn;
+                const Real *Dm = LeanIO<Real>::dk(d) + idm * nn + mbase;
+                double *V = d.vk + idm * nn + mbase;
                 Real djl[NFJ * NFL], djk[NFJ * NFK], dil[NFI * NFL], dik[NFI * NFK];
 #pragma unroll
                 for (int b = 0; b < NFJ; ++b) {

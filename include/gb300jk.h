@@ -64,7 +64,24 @@ typedef struct {
 int jk_opt_create(const int32_t *atm, int natm, const int32_t *bas, int nbas,
                   const double *env, int nenv, double tol, int flags, jk_opt **out);
 
+/* Optimizer for a batch of molecules sharing every class launch (no
+ * counterpart in the reference, which loops over molecules in Python).
+ * The shells of all molecules, each molecule's sorted Cartesian basis, are
+ * merged and sorted by angular momentum; shell_mol[i] is the molecule of
+ * shell i, shell_ao[i] its first AO within that molecule and mol_nao[m] the
+ * AOs of molecule m.  Shell pairs and quartets never mix molecules.
+ * Densities and J/K of a batch are packed: density idm holds, for each
+ * molecule in order, its nao_m x nao_m block (jk_opt_ntot() elements per
+ * density). */
+int jk_opt_create_batch(const int32_t *atm, int natm, const int32_t *bas, int nbas,
+                        const double *env, int nenv, const int32_t *shell_mol,
+                        const int32_t *shell_ao, int nmol, const int32_t *mol_nao,
+                        double tol, int flags, jk_opt **out);
+
 void jk_opt_destroy(jk_opt *opt);
+
+/* Elements per packed density of the optimizer (nao^2 for one molecule). */
+long long jk_opt_ntot(const jk_opt *opt);
 
 /* Number of Cartesian AOs of the sorted basis. */
 int jk_opt_nao(const jk_opt *opt);
@@ -88,6 +105,13 @@ int jk_opt_get_qcond(const jk_opt *opt, double *q);
 int jk_build(jk_opt *opt, const double *dm, int n_dm, int nao, int hermi,
              int with_j, int with_k, int precision, double split_thresh,
              double *vj, double *vk, void *stream, jk_stats *stats);
+
+/* J/K of a batch optimizer: dm, vj, vk are packed [n_dm][jk_opt_ntot()]
+ * (one block per molecule, see jk_opt_create_batch); otherwise as jk_build.
+ * For one molecule it equals jk_build. */
+int jk_build_batch(jk_opt *opt, const double *dm, int n_dm, int hermi,
+                   int with_j, int with_k, int precision, double split_thresh,
+                   double *vj, double *vk, void *stream, jk_stats *stats);
 
 const char *jk_last_error(void);
 
