@@ -30,7 +30,15 @@ static void reg_one(ClassEntry *tab) {
         e.qb64 = e.qb32 = LEAN_THREADS;
         e.smem64 = e.smem32 = 0;
         e.threads64 = e.threads32 = LEAN_THREADS;
+        e.k64_alt = (const void *)rys_class_kernel<LI, LJ, LK, LL, double, MODE_JK>;
+        e.k32_alt = (const void *)rys_class_kernel<LI, LJ, LK, LL, float, MODE_JK>;
+        e.smem64_alt = S64::SMEM;
+        e.smem32_alt = S32::SMEM;
+        e.threads_alt = JK_THREADS;
     } else {
+        e.k64_alt = e.k32_alt = nullptr;
+        e.smem64_alt = e.smem32_alt = 0;
+        e.threads_alt = 0;
         e.lean = 0;
         e.k64 = (const void *)rys_class_kernel<LI, LJ, LK, LL, double, MODE_JK>;
         e.k32 = (const void *)rys_class_kernel<LI, LJ, LK, LL, float, MODE_JK>;

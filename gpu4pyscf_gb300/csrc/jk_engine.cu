@@ -335,6 +335,10 @@ struct jk_opt {
     cudaStream_t side[NSIDE] = {};
     cudaEvent_t fork_ev = nullptr;
     cudaEvent_t join_ev[NSIDE] = {};
+    // autotuned launch variant per (class, precision): kernel family
+    // (0 default, 1 alternative) and grid size in blocks per SM (0: default)
+    int variant_alt[2 * NQCLASS] = {0};
+    int variant_grid[2 * NQCLASS] = {0};
     // per-class timing (diagnostics)
     bool time_classes = false;
     std::vector<cudaEvent_t> ev;        // pairs of events
@@ -430,6 +434,8 @@ int set_smem_attrs() {
         if (e.k64 && !e.lean) CK(cudaFuncSetAttribute(e.k64, cudaFuncAttributeMaxDynamicSharedMemorySize, e.smem64));
         if (e.k32 && !e.lean) CK(cudaFuncSetAttribute(e.k32, cudaFuncAttributeMaxDynamicSharedMemorySize, e.smem32));
         if (e.kdiag) CK(cudaFuncSetAttribute(e.kdiag, cudaFuncAttributeMaxDynamicSharedMemorySize, e.smemdiag));
+        if (e.k64_alt) CK(cudaFuncSetAttribute(e.k64_alt, cudaFuncAttributeMaxDynamicSharedMemorySize, e.smem64_alt));
+        if (e.k32_alt) CK(cudaFuncSetAttribute(e.k32_alt, cudaFuncAttributeMaxDynamicSharedMemorySize, e.smem32_alt));
     }
     return 0;
 }
@@ -455,6 +461,24 @@ int grid_for(const jk_opt *o, long long upper_tiles, int lean = 0) {
     if (upper_tiles < g) g = upper_tiles;
     return (int)std::max<long long>(g, 1);
 }
+
+// Launch the class kernel of (q, prec) with the optimizer's current variant.
+int launch_variant(const jk_opt *o, int q, int prec, long long upper, const EngineDev &d, const ClassDev &c,
+                   cudaStream_t st) {
+    const ClassEntry &e = g_tab[q];
+    const int alt = o->variant_alt[2 * q + prec] && e.k64_alt;
+    const void *k = prec ? (alt ? e.k32_alt : e.k32) : (alt ? e.k64_alt : e.k64);
+    const int smem = prec ? (alt ? e.smem32_alt : e.smem32) : (alt ? e.smem64_alt : e.smem64);
+    const int threads = alt ? e.threads_alt : (prec ? e.threads32 : e.threads64);
+    const int lean = alt ? 0 : e.lean;
+    int grid;
+    if (o->variant_grid[2 * q + prec] > 0)
+        grid = (int)std::max<long long>(1, std::min<long long>(upper, (long long)o->sm_count * o->variant_grid[2 * q + prec]));
+    else
+        grid = grid_for(o, upper, lean);
+    return launch_class(k, grid, smem, d, c, 0, st, threads);
+}
+
 
 }  // namespace
 
@@ -920,7 +944,7 @@ static int build_impl(jk_opt *o, const double *dm, int n_dm, int hermi, int with
         c.work = o->work + 2 * q;
         c.q_off = o->off64[q]; c.ket_begin = o->kb64[q]; c.ket_end = o->ke64[q];
         if (o->time_classes) { o->ev_slot.push_back(2 * q); CK(cudaEventRecord(o->ev[2 * (o->ev_slot.size() - 1)], st)); }
-        if (int er = launch_class(e.k64, grid_for(o, upper, e.lean), e.smem64, d, c, 0, ls, e.threads64)) return er;
+        if (int er = launch_variant(o, q, 0, upper, d, c, ls)) return er;
         if (o->time_classes) CK(cudaEventRecord(o->ev[2 * (o->ev_slot.size() - 1) + 1], st));
         ++launches;
         if (mixed) {
@@ -930,7 +954,7 @@ static int build_impl(jk_opt *o, const double *dm, int n_dm, int hermi, int with
             long long up32 = (long long)o->npairs[a] * ((o->npairs[b] + e.qb32 - 1) / e.qb32 + o->nbk[b]);
             if (o->time_classes) { o->ev_slot.push_back(2 * q + 1); CK(cudaEventRecord(o->ev[2 * (o->ev_slot.size() - 1)], st)); }
             cudaStream_t ls32 = concurrent ? o->side[nlaunched++ % jk_opt::NSIDE] : st;
-            if (int er = launch_class(e.k32, grid_for(o, up32, e.lean), e.smem32, d, c, 0, ls32, e.threads32)) return er;
+            if (int er = launch_variant(o, q, 1, up32, d, c, ls32)) return er;
             if (o->time_classes) CK(cudaEventRecord(o->ev[2 * (o->ev_slot.size() - 1) + 1], st));
             ++launches;
         }
@@ -984,6 +1008,105 @@ int jk_build_batch(jk_opt *o, const double *dm, int n_dm, int hermi, int with_j,
 }
 
 long long jk_opt_ntot(const jk_opt *o) { return o ? o->ntot : -1; }
+
+int jk_opt_set_variant(jk_opt *o, int q, int prec, int alt, int grid_per_sm) {
+    if (!o || q < 0 || q >= NQCLASS || prec < 0 || prec > 1 || alt < 0 || alt > 1 || grid_per_sm < 0 || grid_per_sm > 64)
+        return fail(JK_ERR_ARG, "jk_opt_set_variant: invalid arguments");
+    o->variant_alt[2 * q + prec] = alt;
+    o->variant_grid[2 * q + prec] = grid_per_sm;
+    return 0;
+}
+
+int jk_opt_get_variant(const jk_opt *o, int q, int prec, int *alt, int *grid_per_sm) {
+    if (!o || q < 0 || q >= NQCLASS || prec < 0 || prec > 1 || !alt || !grid_per_sm)
+        return fail(JK_ERR_ARG, "jk_opt_get_variant: invalid arguments");
+    *alt = o->variant_alt[2 * q + prec];
+    *grid_per_sm = o->variant_grid[2 * q + prec];
+    return 0;
+}
+
+// Autotuner: one regular build prepares the screening tables and work
+// ranges for the caller's densities; then every class kernel is relaunched
+// alone for each candidate (kernel family x grid of 1, 2, 4, 8 blocks per
+// SM), timed with CUDA events (best of reps), and the fastest is kept.
+// The internal accumulators are overwritten meanwhile; the caller's data is
+// not touched.  Returns the number of (class, precision) entries tuned.
+int jk_opt_tune(jk_opt *o, const double *dm, int n_dm, int hermi, int precision, double split_thresh,
+                void *stream, int reps) {
+    if (!o || !dm || n_dm <= 0 || reps <= 0) return fail(JK_ERR_ARG, "jk_opt_tune: invalid arguments");
+    cudaStream_t st = (cudaStream_t)stream;
+    double *vj = nullptr, *vk = nullptr;
+    if (int e = dalloc(&vj, (size_t)o->ntot * n_dm)) return e;
+    if (int e = dalloc(&vk, (size_t)o->ntot * n_dm)) { cudaFree(vj); return e; }
+    const bool saved_timing = o->time_classes;
+    o->time_classes = false;
+    int err = build_impl(o, dm, n_dm, hermi, 1, 1, precision, split_thresh, vj, vk, stream, nullptr);
+    o->time_classes = saved_timing;
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    int tuned = 0;
+    if (!err && (cudaEventCreate(&e0) != cudaSuccess || cudaEventCreate(&e1) != cudaSuccess))
+        err = fail(JK_ERR_CUDA, "jk_opt_tune: event creation");
+    const int mixed = precision != JK_PREC_FP64;
+    EngineDev d = base_engine(o);
+    d.dm_cond = o->dm_cond;
+    d.dmj = o->dmj; d.dmk = o->dmk; d.dmj_f = o->dmj_f; d.dmk_f = o->dmk_f;
+    d.vj = o->jt; d.vk = o->kt;
+    d.n_dm = n_dm; d.n_dmk = hermi == 0 ? 2 * n_dm : n_dm;
+    d.with_j = hermi != 2;
+    d.with_k = 1;
+    d.log_cut = o->tol > 0 ? (float)std::log(o->tol) : -1e30f;
+    d.fp32_asym = precision == JK_PREC_MIXED_FP32ROOTS;
+    static const int grids[4] = {1, 2, 4, 8};
+    for (size_t t = 0; !err && t < o->plan_classes.size(); ++t) {
+        const int q = o->plan_classes[t];
+        const ClassEntry &e = g_tab[q];
+        int a = 0;
+        while ((a + 1) * (a + 2) / 2 <= q) ++a;
+        const int b = q - a * (a + 1) / 2;
+        ClassDev c;
+        std::memset(&c, 0, sizeof(c));
+        c.bra = PairList{o->npairs[a], o->pl_ij[a], o->pl_logq[a], o->pl_prim[a]};
+        c.ket = PairList{o->npairs[b], o->pl_ij[b], o->pl_logq[b], o->pl_prim[b]};
+        c.same = a == b;
+        c.nbk = o->nbk[b];
+        c.nx = o->npairs[a] * o->nbk[b];
+        const long long upper = (long long)o->npairs[a] * ((o->npairs[b] + 127) / 128 + o->nbk[b]);
+        for (int prec = 0; prec <= mixed && !err; ++prec) {
+            c.class_id = prec ? NQCLASS + q : q;
+            c.work = o->work + 2 * q + prec;
+            c.q_off = prec ? o->off32[q] : o->off64[q];
+            c.ket_begin = prec ? o->kb32[q] : o->kb64[q];
+            c.ket_end = prec ? o->ke32[q] : o->ke64[q];
+            float best = 1e30f;
+            int best_alt = 0, best_grid = 0;
+            for (int alt = 0; alt <= (e.k64_alt ? 1 : 0) && !err; ++alt)
+                for (int gi = 0; gi < 4 && !err; ++gi) {
+                    o->variant_alt[2 * q + prec] = alt;
+                    o->variant_grid[2 * q + prec] = grids[gi];
+                    float tmin = 1e30f;
+                    for (int r = 0; r < reps && !err; ++r) {
+                        float ms = 0.f;
+                        if (cudaMemsetAsync(c.work, 0, sizeof(int), st) != cudaSuccess ||
+                            cudaEventRecord(e0, st) != cudaSuccess) { err = fail(JK_ERR_CUDA, "jk_opt_tune: record"); break; }
+                        if ((err = launch_variant(o, q, prec, upper, d, c, st))) break;
+                        if (cudaEventRecord(e1, st) != cudaSuccess || cudaEventSynchronize(e1) != cudaSuccess ||
+                            cudaEventElapsedTime(&ms, e0, e1) != cudaSuccess) { err = fail(JK_ERR_CUDA, "jk_opt_tune: timing"); break; }
+                        tmin = std::min(tmin, ms);
+                    }
+                    if (tmin < best) { best = tmin; best_alt = alt; best_grid = grids[gi]; }
+                }
+            o->variant_alt[2 * q + prec] = best_alt;
+            o->variant_grid[2 * q + prec] = best_grid;
+            ++tuned;
+        }
+    }
+    if (e0) cudaEventDestroy(e0);
+    if (e1) cudaEventDestroy(e1);
+    cudaStreamSynchronize(st);
+    cudaFree(vj);
+    cudaFree(vk);
+    return err ? err : 0;
+}
 
 }  // extern "C"
 

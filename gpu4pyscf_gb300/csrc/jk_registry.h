@@ -20,6 +20,11 @@ struct ClassEntry {
     const void *k64;     // FP64 J/K kernel
     const void *k32;     // FP32 J/K kernel
     const void *kdiag;   // Schwarz kernel (bra class == ket class only)
+    // alternative kernel family for the autotuner (block-cooperative kernel of
+    // a class that defaults to the register-resident one; null otherwise)
+    const void *k64_alt;
+    const void *k32_alt;
+    int smem64_alt, smem32_alt, threads_alt;
 };
 
 // Defined in the instantiation translation units, one per bra pair class.

@@ -14,6 +14,7 @@ LIB_PATH = os.path.join(_HERE, 'libgb300jk.so')
 JK_PREC_FP64 = 0
 JK_PREC_MIXED = 1
 JK_PREC_MIXED_FP32ROOTS = 2
+PRECISIONS = {'fp64': JK_PREC_FP64, 'mixed': JK_PREC_MIXED, 'mixed-fp32roots': JK_PREC_MIXED_FP32ROOTS}
 
 
 class JKStats(ctypes.Structure):
@@ -36,7 +37,8 @@ _lock = threading.Lock()
 EXPORTS = ('jk_opt_create', 'jk_opt_destroy', 'jk_opt_nao', 'jk_opt_npairs',
            'jk_opt_get_qcond', 'jk_build', 'jk_last_error', 'jk_n_quartet_classes',
            'jk_opt_time_classes', 'jk_opt_class_times', 'jk_probe_fma', 'jk_int1e',
-           'jk_int1e_last_error')
+           'jk_int1e_last_error', 'jk_opt_create_batch', 'jk_build_batch', 'jk_opt_ntot',
+           'jk_opt_tune', 'jk_opt_set_variant', 'jk_opt_get_variant')
 
 
 def load(path=None):
@@ -78,6 +80,20 @@ def load(path=None):
         lib.jk_int1e.restype = i32
         lib.jk_int1e_last_error.argtypes = []
         lib.jk_int1e_last_error.restype = ctypes.c_char_p
+        lib.jk_opt_create_batch.argtypes = [vp, i32, vp, i32, vp, i32, vp, vp, i32, vp, dp, i32,
+                                            ctypes.POINTER(vp)]
+        lib.jk_opt_create_batch.restype = i32
+        lib.jk_build_batch.argtypes = [vp, vp, i32, i32, i32, i32, i32, dp, vp, vp, vp,
+                                       ctypes.POINTER(JKStats)]
+        lib.jk_build_batch.restype = i32
+        lib.jk_opt_ntot.argtypes = [vp]
+        lib.jk_opt_ntot.restype = ctypes.c_longlong
+        lib.jk_opt_tune.argtypes = [vp, vp, i32, i32, i32, dp, vp, i32]
+        lib.jk_opt_tune.restype = i32
+        lib.jk_opt_set_variant.argtypes = [vp, i32, i32, i32, i32]
+        lib.jk_opt_set_variant.restype = i32
+        lib.jk_opt_get_variant.argtypes = [vp, i32, i32, vp, vp]
+        lib.jk_opt_get_variant.restype = i32
         _lib = lib
         return lib
 

@@ -140,8 +140,7 @@ class _VHFOpt:
         n_dm, nao = dms.shape[0], dms.shape[-1]
         vj = torch.empty_like(dms) if with_j else None
         vk = torch.empty_like(dms) if with_k else None
-        prec = {'fp64': libjk.JK_PREC_FP64, 'mixed': libjk.JK_PREC_MIXED,
-                'mixed-fp32roots': libjk.JK_PREC_MIXED_FP32ROOTS}[self.precision]
+        prec = libjk.PRECISIONS[self.precision]
         st = libjk.JKStats() if stats else None
         stream = torch.cuda.current_stream().cuda_stream
         err = libjk.load().jk_build(self._handle, dms.data_ptr(), n_dm, nao, int(hermi),
@@ -153,6 +152,22 @@ class _VHFOpt:
         if stats:
             self.last_stats = st.as_dict()
         return vj, vk
+
+    def tune(self, dm, hermi=1, reps=3):
+        """Autotune each class's kernel family and grid on user-basis
+        density dm (jk_opt_tune); later builds use the choices."""
+        if self.sorted_mol is None:
+            self.build()
+        dms = self.apply_coeff_C_mat_CT(_as_device(dm).reshape(-1, self.mol.nao, self.mol.nao)).contiguous()
+        err = libjk.load().jk_opt_tune(self._handle, dms.data_ptr(), dms.shape[0], int(hermi),
+                                       libjk.PRECISIONS[self.precision], float(self.split_thresh),
+                                       torch.cuda.current_stream().cuda_stream, int(reps))
+        libjk.check(err, 'jk_opt_tune')
+        return self
+
+    def set_variant(self, q, prec, alt, grid_per_sm):
+        libjk.check(libjk.load().jk_opt_set_variant(self._handle, q, prec, alt, grid_per_sm),
+                    'jk_opt_set_variant')
 
     def get_jk(self, dms, hermi, verbose=None, stats=False):
         """J and K for densities in the sorted basis (jk.py:492-641)."""

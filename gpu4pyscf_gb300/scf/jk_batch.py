@@ -70,16 +70,6 @@ class BatchJK:
         self.mol_base = np.append(0, np.cumsum(self.mol_nao.astype(np.int64) ** 2))
         self.ntot = int(self.mol_base[-1])
         lib = libjk.load()
-        lib.jk_opt_create_batch.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p, ctypes.c_int,
-                                            ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p,
-                                            ctypes.c_int, ctypes.c_void_p, ctypes.c_double, ctypes.c_int,
-                                            ctypes.POINTER(ctypes.c_void_p)]
-        lib.jk_opt_create_batch.restype = ctypes.c_int
-        lib.jk_build_batch.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int, ctypes.c_int,
-                                       ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_double,
-                                       ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
-                                       ctypes.POINTER(libjk.JKStats)]
-        lib.jk_build_batch.restype = ctypes.c_int
         h = ctypes.c_void_p()
         torch.cuda.current_device()
         err = lib.jk_opt_create_batch(self._atm.ctypes.data, len(self._atm), self._bas.ctypes.data,
@@ -121,8 +111,7 @@ class BatchJK:
         n_dm = packed.shape[0]
         vj = torch.empty_like(packed) if with_j else None
         vk = torch.empty_like(packed) if with_k else None
-        prec = {'fp64': libjk.JK_PREC_FP64, 'mixed': libjk.JK_PREC_MIXED,
-                'mixed-fp32roots': libjk.JK_PREC_MIXED_FP32ROOTS}[self.precision]
+        prec = libjk.PRECISIONS[self.precision]
         st = libjk.JKStats() if stats else None
         err = libjk.load().jk_build_batch(self._handle, packed.data_ptr(), n_dm, int(hermi), int(with_j),
                                           int(with_k), prec, float(self.split_thresh),
@@ -147,6 +136,20 @@ class BatchJK:
         js = [C.T @ v @ C for C, v in zip(self._coeff, self.unpack(vj, counts))]
         ks = [C.T @ v @ C for C, v in zip(self._coeff, self.unpack(vk, counts))]
         return js, ks
+
+    def tune(self, dms, hermi=1, reps=3):
+        """Autotune the launch of every class on these densities
+        (jk_opt_tune); later builds use the choices."""
+        dms = [torch.as_tensor(np.asarray(d) if not isinstance(d, torch.Tensor) else d,
+                               dtype=torch.float64, device='cuda') for d in dms]
+        dms = [d if d.ndim == 3 else d[None] for d in dms]
+        n_dm = max(d.shape[0] for d in dms)
+        packed = self.pack([C @ d @ C.T for C, d in zip(self._coeff, dms)], n_dm)
+        err = libjk.load().jk_opt_tune(self._handle, packed.data_ptr(), n_dm, int(hermi),
+                                       libjk.PRECISIONS[self.precision], float(self.split_thresh),
+                                       torch.cuda.current_stream().cuda_stream, int(reps))
+        libjk.check(err, 'jk_opt_tune')
+        return self
 
     # -- CUDA graph -----------------------------------------------------------
     def capture(self, dms, hermi=1):

@@ -113,6 +113,20 @@ int jk_build_batch(jk_opt *opt, const double *dm, int n_dm, int hermi,
                    int with_j, int with_k, int precision, double split_thresh,
                    double *vj, double *vk, void *stream, jk_stats *stats);
 
+/* Autotuner (no counterpart in the reference, whose launch schemes are
+ * fixed per class).  jk_opt_tune times, for every angular class (and
+ * precision) the optimizer launches, each kernel family the class has
+ * (register-resident, block-cooperative) with grids of 1, 2, 4 and 8 blocks
+ * per SM on the given densities (best of reps launches) and keeps the
+ * fastest for later builds.  dm as in jk_build_batch.  Synchronises.
+ * jk_opt_set_variant / jk_opt_get_variant set or read the choice of class
+ * q (0 .. jk_n_quartet_classes()-1) and precision prec (0 FP64, 1 FP32):
+ * alt 0 default family, 1 the alternative; grid_per_sm 0 = default. */
+int jk_opt_tune(jk_opt *opt, const double *dm, int n_dm, int hermi, int precision,
+                double split_thresh, void *stream, int reps);
+int jk_opt_set_variant(jk_opt *opt, int q, int prec, int alt, int grid_per_sm);
+int jk_opt_get_variant(const jk_opt *opt, int q, int prec, int *alt, int *grid_per_sm);
+
 const char *jk_last_error(void);
 
 /* One-electron integrals over the raw Cartesian functions of a sorted basis

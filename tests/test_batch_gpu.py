@@ -71,3 +71,32 @@ def test_batch_graph_replay():
         ref = b.get_jk(dms)
         for a, r in zip(out[0] + out[1], ref[0] + ref[1]):
             assert abs(a - r).max().item() < 1e-11
+
+
+def test_variants_and_autotune_keep_results():
+    """Every launch variant the autotuner can pick gives the same J/K (the
+    pattern of the reference's scheme monkeypatch test,
+    gpu4pyscf/scf/tests/test_scf_j_engine.py:75-93)."""
+    import torch
+    from gpu4pyscf_gb300.lib import libjk
+    from gpu4pyscf_gb300.scf import jk
+    mol = gto.M(atom='O 0 0 0; C 0 1.2 0.2; H 0.9 -0.4 0.3; N 2.4 0.8 -0.3', basis='syn-def2-tzvp')
+    rng = np.random.default_rng(4)
+    dm = rng.random((mol.nao, mol.nao)) - .4
+    dm = dm + dm.T
+    opt = jk._VHFOpt(mol).build()
+    ref_j, ref_k = jk.get_jk(mol, dm, hermi=1, vhfopt=opt)
+    nq = libjk.load().jk_n_quartet_classes()
+    for alt, grid in ((1, 0), (0, 1), (1, 3), (0, 8)):
+        for q in range(nq):
+            opt.set_variant(q, 0, alt, grid)
+        vj, vk = jk.get_jk(mol, dm, hermi=1, vhfopt=opt)
+        assert abs(vj - ref_j).max().item() < 1e-11, (alt, grid)
+        assert abs(vk - ref_k).max().item() < 1e-11, (alt, grid)
+    for q in range(nq):
+        opt.set_variant(q, 0, 0, 0)
+    opt.tune(dm)
+    vj, vk = jk.get_jk(mol, dm, hermi=1, vhfopt=opt)
+    assert abs(vj - ref_j).max().item() < 1e-11
+    assert abs(vk - ref_k).max().item() < 1e-11
+    torch.cuda.synchronize()
