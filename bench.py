@@ -181,6 +181,86 @@ def fma_peak(lib, fp32):
     return best
 
 
+def make_batch(nmol=64, seed=0):
+    """64 seeded molecules of 5-40 atoms (uniform count, C/N/O/H in the
+    proportions of C10N3O5H12), syn-6-31g*, each with 1-4 random symmetric
+    PSD densities X X^T scaled to tr(D S) = N_e."""
+    import torch
+    from gpu4pyscf_gb300.gto import molgen
+    from gpu4pyscf_gb300.scf import hf, jk
+    rng = np.random.default_rng(seed)
+    mols, dms = [], []
+    for m in range(nmol):
+        natm = int(rng.integers(5, 41))
+        mol = molgen.make_mol(molgen.formula_for(natm, rng), 1000 + m, 'syn-6-31g*')
+        opt = jk._VHFOpt(mol).build()
+        S, _, _ = hf.int1e_sorted(opt)
+        C = opt.coeff
+        S = (C.T @ S @ C).cpu().numpy()
+        k = int(rng.integers(1, 5))
+        x = rng.normal(size=(k, mol.nao, mol.nao))
+        d = x @ x.transpose(0, 2, 1)
+        for i in range(k):
+            d[i] *= mol.nelectron / np.trace(d[i] @ S)
+        mols.append((mol, opt))
+        dms.append(d)
+    return mols, dms
+
+
+def run_batched(steps, warmup):
+    """Batched J/K of 64 molecules: per-molecule loop vs shared class
+    launches (eager) vs one CUDA-graph replay after autotuning."""
+    import torch
+    from gpu4pyscf_gb300.scf import jk, jk_batch
+    mols, dms = make_batch()
+
+    def timed_wall(fn, n):
+        ts = []
+        for _ in range(n):
+            torch.cuda.synchronize()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record()
+            fn()
+            e1.record()
+            torch.cuda.synchronize()
+            ts.append(e0.elapsed_time(e1) * 1e-3)
+        return float(np.median(ts))
+
+    dms_dev = [torch.as_tensor(d, device='cuda') for d in dms]
+    loop = lambda: [jk.get_jk(m, d, hermi=1, vhfopt=o) for (m, o), d in zip(mols, dms_dev)]
+    for _ in range(warmup):
+        loop()
+    t_loop = timed_wall(loop, steps)
+    b = jk_batch.BatchJK([m for m, _ in mols])
+    eager = lambda: b.get_jk(dms_dev)
+    for _ in range(warmup):
+        eager()
+    t_eager = timed_wall(eager, steps)
+    b.get_jk(dms_dev, stats=True)
+    nquart = b.last_stats['quartets_fp64']
+    t0 = time.perf_counter()
+    b.tune(dms_dev)
+    t_tune = time.perf_counter() - t0
+    for _ in range(warmup):
+        eager()
+    t_tuned = timed_wall(eager, steps)
+    b.capture(dms_dev)
+    for _ in range(warmup):
+        b.replay()
+    t_graph = timed_wall(b.replay, steps)
+    ref = loop()
+    out = b.replay()
+    torch.cuda.synchronize()
+    err = max(float(abs(a - r).max().item()) for a, r in zip(out[0] + out[1], [x[0] for x in ref] + [x[1] for x in ref]))
+    return {'workload': '64 seeded C/N/O/H molecules of 5-40 atoms, syn-6-31g*, 1-4 random PSD densities each',
+            'n_molecules': len(mols), 'n_densities': int(sum(d.shape[0] for d in dms)),
+            'nao_total': int(sum(m.nao for m, _ in mols)), 'quartets': int(nquart),
+            's_per_batch_molecule_loop': t_loop, 's_per_batch_shared_launches': t_eager,
+            's_per_batch_tuned': t_tuned, 's_per_batch_graph_replay': t_graph,
+            'speedup_graph_vs_loop': t_loop / t_graph, 'autotune_s': t_tune,
+            'quartets_per_s_graph': nquart / t_graph, 'max_abs_diff_vs_loop': err}
+
+
 def run_gpu(args):
     import torch
     import torch.distributed as dist
@@ -353,6 +433,10 @@ def run_gpu(args):
     e2e_val = st64['quartets_fp64'] * world / (sum(te) / args.steps)
     nbytes = dm_host.numel() * 8
 
+    batched = None
+    if not args.no_batch:
+        batched = run_batched(max(3, args.steps), max(2, args.warmup))
+
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu:
         cpu = cpu_sample(mol, dm, target_s=args.cpu_seconds)
@@ -373,7 +457,7 @@ def run_gpu(args):
                         'd2h_bytes_per_step': 2 * nbytes, 's_per_step': sum(te) / args.steps},
                 'gpu_launches': int(st64['kernel_launches']) * args.steps,
                 'mixed': mixed, 'roofline': roofline, 'classes_top': per_class[:8],
-                'cpu_baseline': cpu, 'clocks': clock_info}
+                'batched': batched, 'cpu_baseline': cpu, 'clocks': clock_info}
         print(json.dumps(line))
     if world > 1:
         dist.destroy_process_group()
@@ -390,6 +474,7 @@ def main():
     ap.add_argument('--cpu-seconds', type=float, default=15.)
     ap.add_argument('--ref-seconds', type=float, default=20.)
     ap.add_argument('--no-cpu', action='store_true')
+    ap.add_argument('--no-batch', action='store_true')
     args = ap.parse_args()
     if args.impl == 'reference':
         run_reference(args)

@@ -58,7 +58,7 @@ def test_library_exports_header_symbols():
     from gpu4pyscf_gb300.lib import libjk
     lib = libjk.load()
     hdr = open(os.path.join(ROOT, 'include', 'gb300jk.h')).read()
-    names = re.findall(r'^\s*(?:const\s+)?\w+\s*\*?\s*(jk_\w+)\s*\(', hdr, re.M)
+    names = re.findall(r'^[A-Za-z_][\w \*]*?\b(jk_\w+)\s*\(', hdr, re.M)
     assert set(libjk.EXPORTS) <= set(names)
     for n in names:
         assert hasattr(lib, n), n
