@@ -238,8 +238,12 @@ def run_batched(steps, warmup):
     t_eager = timed_wall(eager, steps)
     b.get_jk(dms_dev, stats=True)
     nquart = b.last_stats['quartets_fp64']
+    # autotune on the first 8 molecules (same classes, an eighth of the work)
+    # and carry the per-class choices over to the full batch
     t0 = time.perf_counter()
-    b.tune(dms_dev)
+    small = jk_batch.BatchJK([m for m, _ in mols[:8]])
+    small.tune(dms_dev[:8], reps=1)
+    b.set_variants(small.variants())
     t_tune = time.perf_counter() - t0
     for _ in range(warmup):
         eager()
@@ -435,7 +439,7 @@ def run_gpu(args):
 
     batched = None
     if not args.no_batch:
-        batched = run_batched(max(3, args.steps), max(2, args.warmup))
+        batched = run_batched(2, 1)
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu:

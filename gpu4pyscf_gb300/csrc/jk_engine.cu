@@ -313,6 +313,8 @@ struct jk_opt {
     std::vector<int> mol_nao_h;
     long long *mol_base = nullptr;
     int *mol_nao = nullptr;
+    int *mol_ndm = nullptr;      // device copy of the per-molecule density counts
+    bool use_mol_ndm = false;
     std::vector<double> qcond_h;  // [nbas*nbas]
     // planning buffers per quartet class
     int *kb64[NQCLASS] = {nullptr}, *ke64[NQCLASS] = {nullptr}, *cnt64[NQCLASS] = {nullptr}, *off64[NQCLASS] = {nullptr};
@@ -449,6 +451,7 @@ EngineDev base_engine(const jk_opt *o) {
     d.rys_coef = o->rys_coef; d.rys_coef_f = o->rys_coef_f;
     d.nbas = o->nbas; d.nao = o->nao;
     d.ntot = o->ntot; d.mol_base = o->mol_base; d.mol_nao = o->mol_nao;
+    d.mol_ndm = o->use_mol_ndm ? o->mol_ndm : nullptr;
     return d;
 }
 
@@ -624,6 +627,7 @@ static int create_impl(const int32_t *atm, int natm, const int32_t *bas, int nba
     }
     if (int e = own_upload(o, &o->mol_base, o->mol_base_h)) return bail(e);
     if (int e = own_upload(o, &o->mol_nao, o->mol_nao_h)) return bail(e);
+    if (int e = own_alloc(o, &o->mol_ndm, (size_t)nmol)) return bail(e);
     if (int e = own_upload(o, &o->shells, o->shells_h)) return bail(e);
     {
         std::vector<double> t(rys_coef_host, rys_coef_host + RYS_TABLE_SIZE);
@@ -1008,6 +1012,16 @@ int jk_build_batch(jk_opt *o, const double *dm, int n_dm, int hermi, int with_j,
 }
 
 long long jk_opt_ntot(const jk_opt *o) { return o ? o->ntot : -1; }
+
+int jk_opt_set_mol_ndm(jk_opt *o, const int32_t *ndm) {
+    if (!o) return fail(JK_ERR_ARG, "jk_opt_set_mol_ndm: null optimizer");
+    if (!ndm) { o->use_mol_ndm = false; return 0; }
+    for (int m = 0; m < o->nmol; ++m)
+        if (ndm[m] < 0) return fail(JK_ERR_ARG, "jk_opt_set_mol_ndm: negative count");
+    CK(cudaMemcpy(o->mol_ndm, ndm, sizeof(int) * o->nmol, cudaMemcpyHostToDevice));
+    o->use_mol_ndm = true;
+    return 0;
+}
 
 int jk_opt_set_variant(jk_opt *o, int q, int prec, int alt, int grid_per_sm) {
     if (!o || q < 0 || q >= NQCLASS || prec < 0 || prec > 1 || alt < 0 || alt > 1 || grid_per_sm < 0 || grid_per_sm > 64)

@@ -390,6 +390,7 @@ rys_class_kernel(EngineDev d, ClassDev c, int ntiles_static)
                 const int mol = d.shells[si.ish].mol;
                 const int nao = __ldg(d.mol_nao + mol);
                 const size_t mbase = (size_t)__ldg(d.mol_base + mol);
+                const int ndm_m = d.mol_ndm ? __ldg(d.mol_ndm + mol) : d.n_dm;
                 const Real *Es = E + s * NF;
                 const int ai = d.shells[si.ish].ao, aj = d.shells[si.jsh].ao;
                 const int ak = d.shells[si.ksh].ao, al = d.shells[si.lsh].ao;
@@ -397,6 +398,7 @@ rys_class_kernel(EngineDev d, ClassDev c, int ntiles_static)
                 double *out;
                 if (t < nj) {
                     int idm = t / NJ, o = t % NJ;
+                    if (idm >= ndm_m) continue;  // density the molecule does not carry
                     const Real *D = dm_ptr<Real>(d, true, idm) + mbase;
                     if (o < NFI * NFJ) {
                         int a = o / NFJ, b = o % NFJ;
@@ -417,6 +419,7 @@ rys_class_kernel(EngineDev d, ClassDev c, int ntiles_static)
                 } else {
                     t -= nj;
                     int idm = t / NK, o = t % NK;
+                    if (idm % d.n_dm >= ndm_m) continue;
                     const Real *D = dm_ptr<Real>(d, false, idm) + mbase;
                     double *V = d.vk + (size_t)idm * d.ntot + mbase;
                     if (o < NFI * NFK) {            // K[i a, k c] += E[abcd] D[j b, l d]

@@ -273,12 +273,16 @@ rys_lean_kernel(EngineDev d, ClassDev c, int unused)
         const int nao = __ldg(d.mol_nao + mol);
         const size_t nn = (size_t)d.ntot;
         const size_t mbase = (size_t)__ldg(d.mol_base + mol);
+        const int ndm_m = d.mol_ndm ? __ldg(d.mol_ndm + mol) : d.n_dm;
         const Real fac = Real((pij.x == pij.y ? .5 : 1.) * (pkl.x == pkl.y ? .5 : 1.) *
                               (c.same && ib == ket ? .5 : 1.));
         const int ai = A.ao, aj = B.ao;
         const int ak = valid ? d.shells[pkl.x].ao : 0, al = valid ? d.shells[pkl.y].ao : 0;
         if (d.with_j) {
             for (int idm = 0; idm < d.n_dm; ++idm) {
+                // densities the molecule does not carry are skipped
+                const bool vd = valid && idm < ndm_m;
+                if (!__any_sync(0xffffffffu, vd)) continue;
                 const Real *Dm = LeanIO<Real>::dj(d) + idm * nn + mbase;
                 double *V = d.vj + idm * nn + mbase;
                 Real dkl[NFK * NFL], dij[NFI * NFJ];
@@ -286,7 +290,7 @@ rys_lean_kernel(EngineDev d, ClassDev c, int unused)
                 for (int cc = 0; cc < NFK; ++cc)
 #pragma unroll
                     for (int dd = 0; dd < NFL; ++dd)
-                        dkl[cc * NFL + dd] = valid ? Dm[(size_t)(ak + cc) * nao + al + dd] : Real(0);
+                        dkl[cc * NFL + dd] = vd ? Dm[(size_t)(ak + cc) * nao + al + dd] : Real(0);
 #pragma unroll
                 for (int a = 0; a < NFI; ++a)
 #pragma unroll
@@ -297,17 +301,17 @@ rys_lean_kernel(EngineDev d, ClassDev c, int unused)
                     Real s = Real(0);
 #pragma unroll
                     for (int cd = 0; cd < NFK * NFL; ++cd) s += acc[ab * NFK * NFL + cd] * dkl[cd];
-                    double sd = valid ? (double)(fac * s) : 0.;
+                    double sd = vd ? (double)(fac * s) : 0.;
                     double *dst = V + (size_t)(ai + ab / NFJ) * nao + aj + ab % NFJ;
                     if (same_bra) {
 #pragma unroll
                         for (int off = 16; off > 0; off >>= 1) sd += __shfl_xor_sync(0xffffffffu, sd, off);
                         if (lane == 0 && sd != 0.) atomicAdd(dst, sd);
-                    } else if (valid) {
+                    } else if (vd) {
                         atomicAdd(dst, sd);
                     }
                 }
-                if (valid) {
+                if (vd) {
 #pragma unroll
                     for (int cd = 0; cd < NFK * NFL; ++cd) {
                         Real s = Real(0);
@@ -322,6 +326,8 @@ rys_lean_kernel(EngineDev d, ClassDev c, int unused)
             // lanes whose kets share a shell hit the same K elements: add
             // through warp aggregation (idle lanes contribute nothing)
             for (int idm = 0; idm < d.n_dmk; ++idm) {
+                const bool vd = valid && (idm % d.n_dm) < ndm_m;
+                if (!__any_sync(0xffffffffu, vd)) continue;
                 const Real *Dm = LeanIO<Real>::dk(d) + idm * nn + mbase;
                 double *V = d.vk + idm * nn + mbase;
                 Real djl[NFJ * NFL], djk[NFJ * NFK], dil[NFI * NFL], dik[NFI * NFK];
@@ -348,7 +354,7 @@ rys_lean_kernel(EngineDev d, ClassDev c, int unused)
                         for (int b = 0; b < NFJ; ++b)
 #pragma unroll
                             for (int dd = 0; dd < NFL; ++dd) s += acc[((a * NFJ + b) * NFK + cc) * NFL + dd] * djl[b * NFL + dd];
-                        warp_agg_add(valid ? V + (size_t)(ai + a) * nao + ak + cc : nullptr, (double)(fac * s), ab_buf, lane);
+                        warp_agg_add(vd ? V + (size_t)(ai + a) * nao + ak + cc : nullptr, (double)(fac * s), ab_buf, lane);
                     }
 #pragma unroll
                 for (int a = 0; a < NFI; ++a)
@@ -359,7 +365,7 @@ rys_lean_kernel(EngineDev d, ClassDev c, int unused)
                         for (int b = 0; b < NFJ; ++b)
 #pragma unroll
                             for (int cc = 0; cc < NFK; ++cc) s += acc[((a * NFJ + b) * NFK + cc) * NFL + dd] * djk[b * NFK + cc];
-                        warp_agg_add(valid ? V + (size_t)(ai + a) * nao + al + dd : nullptr, (double)(fac * s), ab_buf, lane);
+                        warp_agg_add(vd ? V + (size_t)(ai + a) * nao + al + dd : nullptr, (double)(fac * s), ab_buf, lane);
                     }
 #pragma unroll
                 for (int b = 0; b < NFJ; ++b)
@@ -370,7 +376,7 @@ rys_lean_kernel(EngineDev d, ClassDev c, int unused)
                         for (int a = 0; a < NFI; ++a)
 #pragma unroll
                             for (int dd = 0; dd < NFL; ++dd) s += acc[((a * NFJ + b) * NFK + cc) * NFL + dd] * dil[a * NFL + dd];
-                        warp_agg_add(valid ? V + (size_t)(aj + b) * nao + ak + cc : nullptr, (double)(fac * s), ab_buf, lane);
+                        warp_agg_add(vd ? V + (size_t)(aj + b) * nao + ak + cc : nullptr, (double)(fac * s), ab_buf, lane);
                     }
 #pragma unroll
                 for (int b = 0; b < NFJ; ++b)
@@ -381,7 +387,7 @@ rys_lean_kernel(EngineDev d, ClassDev c, int unused)
                         for (int a = 0; a < NFI; ++a)
 #pragma unroll
                             for (int cc = 0; cc < NFK; ++cc) s += acc[((a * NFJ + b) * NFK + cc) * NFL + dd] * dik[a * NFK + cc];
-                        warp_agg_add(valid ? V + (size_t)(aj + b) * nao + al + dd : nullptr, (double)(fac * s), ab_buf, lane);
+                        warp_agg_add(vd ? V + (size_t)(aj + b) * nao + al + dd : nullptr, (double)(fac * s), ab_buf, lane);
                     }
             }
         }

@@ -131,11 +131,36 @@ class BatchJK:
         dms = [d if d.ndim == 3 else d[None] for d in dms]
         counts = [d.shape[0] for d in dms]
         n_dm = max(counts)
+        self._set_counts(counts)
         ds = [C @ d @ C.T for C, d in zip(self._coeff, dms)]
         vj, vk = self.build_sorted(self.pack(ds, n_dm), hermi, stats=stats)
         js = [C.T @ v @ C for C, v in zip(self._coeff, self.unpack(vj, counts))]
         ks = [C.T @ v @ C for C, v in zip(self._coeff, self.unpack(vk, counts))]
         return js, ks
+
+    def _set_counts(self, counts):
+        counts = tuple(int(c) for c in counts)
+        if getattr(self, '_counts', None) != counts:
+            arr = np.asarray(counts, dtype=np.int32)
+            libjk.check(libjk.load().jk_opt_set_mol_ndm(self._handle, arr.ctypes.data), 'jk_opt_set_mol_ndm')
+            self._counts = counts
+
+    def variants(self):
+        """Current launch choice (alt, grid) of every (class, precision)."""
+        lib = libjk.load()
+        out = []
+        a, g = ctypes.c_int(), ctypes.c_int()
+        for q in range(lib.jk_n_quartet_classes()):
+            for prec in (0, 1):
+                libjk.check(lib.jk_opt_get_variant(self._handle, q, prec, ctypes.byref(a), ctypes.byref(g)),
+                            'jk_opt_get_variant')
+                out.append((q, prec, a.value, g.value))
+        return out
+
+    def set_variants(self, variants):
+        lib = libjk.load()
+        for q, prec, a, g in variants:
+            libjk.check(lib.jk_opt_set_variant(self._handle, q, prec, a, g), 'jk_opt_set_variant')
 
     def tune(self, dms, hermi=1, reps=3):
         """Autotune the launch of every class on these densities
@@ -144,6 +169,7 @@ class BatchJK:
                                dtype=torch.float64, device='cuda') for d in dms]
         dms = [d if d.ndim == 3 else d[None] for d in dms]
         n_dm = max(d.shape[0] for d in dms)
+        self._set_counts([d.shape[0] for d in dms])
         packed = self.pack([C @ d @ C.T for C, d in zip(self._coeff, dms)], n_dm)
         err = libjk.load().jk_opt_tune(self._handle, packed.data_ptr(), n_dm, int(hermi),
                                        libjk.PRECISIONS[self.precision], float(self.split_thresh),
@@ -160,6 +186,7 @@ class BatchJK:
         self._static_in = [d if d.ndim == 3 else d[None] for d in self._static_in]
         s = torch.cuda.Stream()
         s.wait_stream(torch.cuda.current_stream())
+        self._set_counts([d.shape[0] for d in self._static_in])
         with torch.cuda.stream(s):
             for _ in range(2):  # allocate the workspace before capture
                 self.get_jk(self._static_in, hermi)

@@ -80,6 +80,12 @@ int jk_opt_create_batch(const int32_t *atm, int natm, const int32_t *bas, int nb
 
 void jk_opt_destroy(jk_opt *opt);
 
+/* Densities each molecule of a batch carries (host array [nmol]; NULL
+ * clears): later builds skip the digestion of density slots beyond a
+ * molecule's count, so molecules with fewer densities than the batch's
+ * n_dm cost no more than their own.  Those slots must hold zeros. */
+int jk_opt_set_mol_ndm(jk_opt *opt, const int32_t *ndm);
+
 /* Elements per packed density of the optimizer (nao^2 for one molecule). */
 long long jk_opt_ntot(const jk_opt *opt);
 
