@@ -71,6 +71,7 @@ struct EngineDev {
     long long ntot;
     const long long *mol_base;
     const int *mol_nao;
+    const int *mol_ndm;       // densities each molecule carries (null: all n_dm)
     int with_j, with_k;
     float log_cut;
     int fp32_asym;            // 1: FP32 quartets take the large-T asymptote in FP32 too
