@@ -23,7 +23,7 @@ FLAGS = ['-O3', '-std=c++17', '-lineinfo', '-Xcompiler', '-fPIC', '-diag-suppres
 NBRA = 10
 
 SOURCES = ['jk_device.cuh', 'jk_kernel.cuh', 'rys_roots.cuh', 'rys_tables.inc', 'jk_registry.h',
-           'jk_classes.cu', 'jk_engine.cu', 'int1e.cu', 'build.py']
+           'jk_classes.cu', 'jk_engine.cu', 'int1e.cu', 'mlp.cu', 'build.py']
 
 
 def _digest():
@@ -31,8 +31,9 @@ def _digest():
     for f in SOURCES:
         with open(os.path.join(HERE, f), 'rb') as fh:
             h.update(fh.read())
-    with open(os.path.join(ROOT, 'include', 'gb300jk.h'), 'rb') as fh:
-        h.update(fh.read())
+    for hdr in ('gb300jk.h', 'gb300mlp.h'):
+        with open(os.path.join(ROOT, 'include', hdr), 'rb') as fh:
+            h.update(fh.read())
     h.update(' '.join(ARCH + FLAGS).encode())
     return h.hexdigest()
 
@@ -60,7 +61,7 @@ def build(force=False, verbose=False, jobs=None):
         cmds.append([NVCC] + ARCH + FLAGS + ['-DJK_BRA_CLASS=%d' % b, '-c',
                                              os.path.join(HERE, 'jk_classes.cu'), '-o', o])
         objs.append(o)
-    for src in ('jk_engine.cu', 'int1e.cu'):
+    for src in ('jk_engine.cu', 'int1e.cu', 'mlp.cu'):
         o = os.path.join(BUILD, src.replace('.cu', '.o'))
         cmds.append([NVCC] + ARCH + FLAGS + ['-c', os.path.join(HERE, src), '-o', o])
         objs.append(o)

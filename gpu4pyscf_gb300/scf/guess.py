@@ -121,17 +121,22 @@ def atom_density(symb, shells, cart=False, max_cycle=60, tol=1e-9):
     return dm
 
 
+_ATOM_CACHE = {}
+
+
 def sad_density(mol):
-    """Block-diagonal superposition of atomic densities in mol's AO basis."""
+    """Block-diagonal superposition of atomic densities in mol's AO basis.
+    Atomic densities are cached per (element, basis shells, cart)."""
     from ..gto.mole import std_symbol
     n = mol.nao
     dm = np.zeros((n, n))
-    cache = {}
+    cache = _ATOM_CACHE
     slices = atom_ao_slices(mol)
     for ia in range(mol.natm):
         symb = std_symbol(mol.atom_symbol(ia))
-        if symb not in cache:
-            cache[symb] = atom_density(symb, mol._basis[symb], cart=bool(mol.cart))
+        key = (symb, repr(mol._basis[symb]), bool(mol.cart))
+        if key not in cache:
+            cache[key] = atom_density(symb, mol._basis[symb], cart=bool(mol.cart))
         lo, hi = slices[ia]
-        dm[lo:hi, lo:hi] = cache[symb]
+        dm[lo:hi, lo:hi] = cache[key]
     return dm

@@ -118,6 +118,7 @@ class RHF:
         self.cycles = 0
         self.mo_energy = self.mo_coeff = self.mo_occ = None
         self.scf_summary = {}
+        self.guess_model = None   # learned_guess.GuessModel for init_guess='learned'
         self._opt = None
         self._int1e = None
 
@@ -209,6 +210,10 @@ class RHF:
         if key in ('minao', 'atom', 'sad'):
             dm = guess.sad_density(self.mol)
             return torch.as_tensor(dm, device='cuda')
+        if key == 'learned':
+            if self.guess_model is None:
+                raise ValueError("init_guess='learned' needs RHF.guess_model")
+            return torch.as_tensor(self.guess_model.predict_density(self.mol), device='cuda')
         if key in ('1e', 'hcore', 'core'):
             h = self.get_hcore()
             e, c = self.eig(h)

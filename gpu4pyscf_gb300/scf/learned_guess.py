@@ -1,0 +1,281 @@
+"""Learned initial density from geometry (atom-pair network).
+
+For every atom pair (A <= B) a dense network (3 hidden layers of width 256,
+SiLU, FP32; ``scf/mlp.py`` on the kernels of include/gb300mlp.h) maps
+pair features to the density block D[A, B] in the user AO basis, padded to
+the largest atomic block of the basis.  Features, all in the molecular
+frame: element one-hots of A and B, distance and its decays, the
+displacement and its direction, an element-resolved radial environment of
+each atom (Gaussians at 6 radii per element) and a same-atom flag.  The
+predicted blocks are assembled (D[B, A] = D[A, B]^T, diagonal blocks
+symmetrised) into the starting density of the SCF; the SCF's first Fock
+build and diagonalisation turn it into an idempotent density.
+
+Training data are converged FP64 densities produced by this engine's own
+RHF on seeded conformers (random displacements of seeded base molecules).
+``superposition-of-atoms`` (SAD) stays the default guess; ``RHF.init_guess =
+'learned'`` with ``RHF.guess_model`` set uses the network.
+"""
+
+import json
+import time
+
+import numpy as np
+import torch
+
+from ..gto import M
+from ..gto.mole import charge_of, std_symbol
+from . import guess, hf, mlp
+
+ELEMS = ['H', 'C', 'N', 'O']
+ENV_MU = np.array([1.0, 1.8, 2.6, 3.6, 4.8, 6.5])
+ENV_W = 0.6
+NFEAT = 8 + 3 + 3 + 3 + 2 * 4 * len(ENV_MU) + 1
+
+
+def _atoms(mol):
+    coords = mol.atom_coords()
+    symbs = [std_symbol(mol.atom_symbol(i)) for i in range(mol.natm)]
+    return symbs, coords
+
+
+def pair_features(mol):
+    """(features [npair, NFEAT] float64, pairs [(A, B)])."""
+    symbs, R = _atoms(mol)
+    n = len(symbs)
+    onehot = np.zeros((n, 4))
+    for i, s in enumerate(symbs):
+        onehot[i, ELEMS.index(s)] = 1.
+    dist = np.linalg.norm(R[:, None] - R[None], axis=-1)
+    env = np.zeros((n, 4, len(ENV_MU)))
+    for a in range(n):
+        for c in range(n):
+            if a == c:
+                continue
+            env[a, ELEMS.index(symbs[c])] += np.exp(-(dist[a, c] - ENV_MU) ** 2 / (2 * ENV_W ** 2))
+    env = env.reshape(n, -1)
+    pairs, feats = [], []
+    for a in range(n):
+        for b in range(a, n):
+            d = R[b] - R[a]
+            r = dist[a, b]
+            u = d / r if r > 0 else np.zeros(3)
+            f = np.concatenate([onehot[a], onehot[b], [r, 1. / (1. + r), np.exp(-0.5 * r)], d, u,
+                                env[a], env[b], [1. if a == b else 0.]])
+            pairs.append((a, b))
+            feats.append(f)
+    return np.array(feats), pairs
+
+
+def block_slices(mol):
+    return guess.atom_ao_slices(mol)
+
+
+class GuessModel:
+    """Feature scaling + network + block layout."""
+
+    def __init__(self, nblock, hidden=256, seed=0):
+        self.nblock = nblock
+        self.net = mlp.DenseMLP([NFEAT, hidden, hidden, hidden, nblock * nblock], seed=seed)
+        self.mu = np.zeros(NFEAT)
+        self.sd = np.ones(NFEAT)
+
+    def _x(self, feats):
+        return torch.as_tensor(((feats - self.mu) / self.sd).astype(np.float32), device='cuda')
+
+    def predict_blocks(self, feats):
+        return self.net.forward(self._x(feats), keep=False).cpu().numpy().astype(np.float64)
+
+    def predict_density(self, mol):
+        feats, pairs = pair_features(mol)
+        blocks = self.predict_blocks(feats).reshape(-1, self.nblock, self.nblock)
+        sl = block_slices(mol)
+        dm = np.zeros((mol.nao, mol.nao))
+        for (a, b), blk in zip(pairs, blocks):
+            (a0, a1), (b0, b1) = sl[a], sl[b]
+            x = blk[:a1 - a0, :b1 - b0]
+            if a == b:
+                x = 0.5 * (x + x.T)
+                dm[a0:a1, a0:a1] = x
+            else:
+                dm[a0:a1, b0:b1] = x
+                dm[b0:b1, a0:a1] = x.T
+        return dm
+
+
+def targets(mol, dm, nblock):
+    """Padded density blocks [npair, nblock^2] and their masks."""
+    _, pairs = pair_features(mol)
+    sl = block_slices(mol)
+    T = np.zeros((len(pairs), nblock, nblock))
+    Mk = np.zeros_like(T)
+    for k, (a, b) in enumerate(pairs):
+        (a0, a1), (b0, b1) = sl[a], sl[b]
+        T[k, :a1 - a0, :b1 - b0] = dm[a0:a1, b0:b1]
+        Mk[k, :a1 - a0, :b1 - b0] = 1.
+    return T.reshape(len(pairs), -1), Mk.reshape(len(pairs), -1)
+
+
+# -- data -------------------------------------------------------------------
+def base_formula(rng):
+    nh = int(rng.integers(8, 21))
+    frac = np.array([10, 3, 5], dtype=float) / 18.
+    counts = np.floor(frac * nh).astype(int)
+    while counts.sum() < nh:
+        counts[rng.choice(3, p=frac)] += 1
+    n_h = int(round(0.7 * nh))
+    f = {'C': int(counts[0]), 'N': int(counts[1]), 'O': int(counts[2]), 'H': n_h}
+    if (6 * f['C'] + 7 * f['N'] + 8 * f['O'] + f['H']) % 2:
+        f['H'] += 1
+    return f
+
+
+def make_conformers(nbase, nconf, basis, seed=0, sigma=0.05):
+    """Seeded base molecules (8-20 heavy atoms) and nconf conformers each
+    (Gaussian displacements of sigma Angstrom); returns [[mol, ...], ...]."""
+    from ..gto import molgen
+    rng = np.random.default_rng(seed)
+    out = []
+    for b in range(nbase):
+        f = base_formula(rng)
+        atoms = None
+        s = 7919 * (b + 1) + seed
+        for _ in range(50):
+            try:
+                atoms = molgen.random_molecule(f, s)
+                break
+            except RuntimeError:
+                s += 1000003
+        confs = []
+        for c in range(nconf):
+            disp = rng.normal(scale=sigma, size=(len(atoms), 3))
+            at = [(sym, xyz + d) for (sym, xyz), d in zip(atoms, disp)]
+            confs.append(M(atom=molgen.atom_string(at), basis=basis))
+        out.append(confs)
+    return out
+
+
+def converged_density(mol, dm0=None, conv_tol=1e-9, precision='fp64'):
+    mf = hf.RHF(mol)
+    mf.conv_tol = conv_tol
+    mf.precision = precision
+    mf.kernel(dm0=dm0)
+    return mf
+
+
+def generate(confsets, holdout, conv_tol=1e-9, log=None):
+    """Converged densities of every conformer except the last ``holdout`` of
+    each base molecule (those are kept for evaluation)."""
+    data = []
+    t0 = time.perf_counter()
+    for b, confs in enumerate(confsets):
+        prev = None
+        for c, mol in enumerate(confs[:len(confs) - holdout]):
+            mf = converged_density(mol, dm0=prev, conv_tol=conv_tol)
+            prev = mf.dm.cpu().numpy()
+            data.append((mol, prev))
+        if log:
+            log('base %d: %d conformers, %.1f s' % (b, len(confs) - holdout, time.perf_counter() - t0))
+    return data
+
+
+def build_arrays(data, nblock):
+    Xs, Ts, Ms = [], [], []
+    for mol, dm in data:
+        f, _ = pair_features(mol)
+        t, m = targets(mol, dm, nblock)
+        Xs.append(f)
+        Ts.append(t)
+        Ms.append(m)
+    return np.concatenate(Xs), np.concatenate(Ts), np.concatenate(Ms)
+
+
+def train(data, nblock, epochs=40, batch=4096, lr=1e-3, seed=0, log=None):
+    X, T, Mk = build_arrays(data, nblock)
+    model = GuessModel(nblock, seed=seed)
+    model.mu = X.mean(0)
+    model.sd = X.std(0) + 1e-6
+    Xd = model._x(X)
+    Td = torch.as_tensor(T.astype(np.float32), device='cuda')
+    Md = torch.as_tensor(Mk.astype(np.float32), device='cuda')
+    n = len(X)
+    g = torch.Generator(device='cpu').manual_seed(seed)
+    hist = []
+    steps = epochs * ((n + batch - 1) // batch)
+    step = 0
+    for ep in range(epochs):
+        perm = torch.randperm(n, generator=g).cuda()
+        tot = 0.
+        for i in range(0, n, batch):
+            idx = perm[i:i + batch]
+            rate = lr * 0.5 * (1 + np.cos(np.pi * step / steps))
+            y = model.net.forward(Xd[idx])
+            loss, grad = mlp.mse(y, Td[idx], Md[idx])
+            model.net.backward(grad)
+            model.net.adam_step(lr=float(rate))
+            tot += loss.item() * len(idx)
+            step += 1
+        hist.append(tot / n)
+        if log and (ep % 10 == 0 or ep == epochs - 1):
+            log('epoch %d loss %.3e' % (ep, tot / n))
+    model.loss_history = hist
+    return model
+
+
+def evaluate(model, mols, conv_tol=1e-8):
+    rows = []
+    for mol in mols:
+        a = hf.RHF(mol)
+        a.conv_tol = conv_tol
+        e_sad = a.kernel()
+        b = hf.RHF(mol)
+        b.conv_tol = conv_tol
+        e_ml = b.kernel(dm0=model.predict_density(mol))
+        rows.append({'natm': mol.natm, 'nao': mol.nao, 'cycles_sad': a.cycles, 'cycles_learned': b.cycles,
+                     'e_sad': e_sad, 'e_learned': e_ml, 'converged': bool(a.converged and b.converged)})
+    cs = np.array([r['cycles_sad'] for r in rows])
+    cl = np.array([r['cycles_learned'] for r in rows])
+    de = np.array([abs(r['e_learned'] - r['e_sad']) for r in rows])
+    return {'n': len(rows), 'mean_cycles_sad': float(cs.mean()), 'mean_cycles_learned': float(cl.mean()),
+            'cycle_reduction': float(1 - cl.mean() / cs.mean()), 'max_abs_dE': float(de.max()),
+            'all_converged': all(r['converged'] for r in rows), 'rows': rows}
+
+
+def run(nbase=20, nconf=100, holdout=10, basis='syn-def2-svp', epochs=40, seed=0, out=None):
+    log = lambda m: print(m, flush=True)
+    t0 = time.perf_counter()
+    confsets = make_conformers(nbase, nconf, basis, seed)
+    nblock = max(b - a for cs in confsets for (a, b) in block_slices(cs[0]))
+    data = generate(confsets, holdout, log=log)
+    t_gen = time.perf_counter() - t0
+    t1 = time.perf_counter()
+    model = train(data, nblock, epochs=epochs, seed=seed, log=log)
+    t_train = time.perf_counter() - t1
+    held = [m for cs in confsets for m in cs[len(cs) - holdout:]]
+    t2 = time.perf_counter()
+    res = evaluate(model, held)
+    res.update({'workload': '%d base molecules (8-20 heavy atoms, C/N/O/H) x %d conformers (sigma 0.05 A), %s; '
+                            '%d held out' % (nbase, nconf, basis, len(held)),
+                'train_conformers': len(data), 'train_pairs': int(sum(m.natm * (m.natm + 1) // 2 for m, _ in data)),
+                'final_train_loss': model.loss_history[-1], 'first_train_loss': model.loss_history[0],
+                'generate_s': t_gen, 'train_s': t_train, 'evaluate_s': time.perf_counter() - t2})
+    if out:
+        slim = dict(res)
+        slim['rows'] = res['rows'][:20]
+        with open(out, 'w') as f:
+            json.dump(slim, f, indent=1)
+    return res, model
+
+
+if __name__ == '__main__':
+    import argparse
+    ap = argparse.ArgumentParser()
+    ap.add_argument('--bases', type=int, default=20)
+    ap.add_argument('--conformers', type=int, default=100)
+    ap.add_argument('--holdout', type=int, default=10)
+    ap.add_argument('--epochs', type=int, default=40)
+    ap.add_argument('--basis', default='syn-def2-svp')
+    ap.add_argument('--out', default=None)
+    a = ap.parse_args()
+    res, _ = run(a.bases, a.conformers, a.holdout, a.basis, a.epochs, out=a.out)
+    print(json.dumps({k: v for k, v in res.items() if k != 'rows'}))
