@@ -110,7 +110,10 @@ class RHF:
         self.init_guess = 'minao'
         self.precision = 'fp64'
         self.split_thresh = 1e-6
-        self.level_shift = 0.
+        self.level_shift = 0.        # Ha added to virtual orbital energies
+        self.level_shift_cycles = None  # cycles the shift applies to (None: all)
+        self.damp = 0.                # Fock mixing with the previous cycle's Fock
+        self.damp_cycles = 0
         self.lindep = 1e-8
         self.verbose = 0
         self.converged = False
@@ -244,11 +247,18 @@ class RHF:
         self.converged = False
         dm_last = vhf_last = None
         nbuild = 1
+        fock_prev = None
         for cycle in range(self.max_cycle):
             fock = h1e + vhf
             err = X.T @ (fock @ dm @ s1e - s1e @ dm @ fock) @ X
-            if cycle >= self.diis_start_cycle - 1:
+            if cycle < self.damp_cycles and fock_prev is not None and self.damp > 0:
+                fock = (1 - self.damp) * fock + self.damp * fock_prev
+            elif cycle >= self.diis_start_cycle - 1:
                 fock = diis.update(fock, err)
+            fock_prev = fock
+            if self.level_shift > 0 and (self.level_shift_cycles is None or cycle < self.level_shift_cycles):
+                # shift the virtual space: F + shift (S - S D S / 2)
+                fock = fock + self.level_shift * (s1e - 0.5 * s1e @ dm @ s1e)
             mo_e, mo_c = self.eig(fock)
             mo_occ = self.get_occ(mo_e, mo_c)
             dm_last, vhf_last, e_last = dm, vhf, e_tot
