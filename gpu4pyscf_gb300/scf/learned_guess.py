@@ -2,8 +2,10 @@
 
 For every atom pair (A <= B) a dense network (3 hidden layers of width 256,
 SiLU, FP32; ``scf/mlp.py`` on the kernels of include/gb300mlp.h) maps
-pair features to the density block D[A, B] in the user AO basis, padded to
-the largest atomic block of the basis.  Features, all in the molecular
+pair features to the correction of the density block D[A, B] over the
+superposition-of-atoms (SAD) density, in the user AO basis, padded to the
+largest atomic block of the basis; the guess is SAD plus the predicted
+correction, so an untrained network falls back to SAD.  Features, all in the molecular
 frame: element one-hots of A and B, distance and its decays, the
 displacement and its direction, an element-resolved radial environment of
 each atom (Gaussians at 6 radii per element) and a same-atom flag.  The
@@ -91,6 +93,7 @@ class GuessModel:
         blocks = self.predict_blocks(feats).reshape(-1, self.nblock, self.nblock)
         sl = block_slices(mol)
         dm = np.zeros((mol.nao, mol.nao))
+        base = guess.sad_density(mol)
         for (a, b), blk in zip(pairs, blocks):
             (a0, a1), (b0, b1) = sl[a], sl[b]
             x = blk[:a1 - a0, :b1 - b0]
@@ -100,7 +103,7 @@ class GuessModel:
             else:
                 dm[a0:a1, b0:b1] = x
                 dm[b0:b1, a0:a1] = x.T
-        return dm
+        return base + dm
 
 
 def targets(mol, dm, nblock):
@@ -163,7 +166,7 @@ def converged_density(mol, dm0=None, conv_tol=1e-9, precision='fp64'):
     return mf
 
 
-def generate(confsets, holdout, conv_tol=1e-9, log=None):
+def generate(confsets, holdout, conv_tol=1e-8, log=None):
     """Converged densities of every conformer except the last ``holdout`` of
     each base molecule (those are kept for evaluation)."""
     data = []
@@ -183,7 +186,7 @@ def build_arrays(data, nblock):
     Xs, Ts, Ms = [], [], []
     for mol, dm in data:
         f, _ = pair_features(mol)
-        t, m = targets(mol, dm, nblock)
+        t, m = targets(mol, dm - guess.sad_density(mol), nblock)
         Xs.append(f)
         Ts.append(t)
         Ms.append(m)
@@ -241,7 +244,7 @@ def evaluate(model, mols, conv_tol=1e-8):
             'all_converged': all(r['converged'] for r in rows), 'rows': rows}
 
 
-def run(nbase=20, nconf=100, holdout=10, basis='syn-def2-svp', epochs=40, seed=0, out=None):
+def run(nbase=10, nconf=60, holdout=10, basis='syn-def2-svp', epochs=60, seed=0, out=None):
     log = lambda m: print(m, flush=True)
     t0 = time.perf_counter()
     confsets = make_conformers(nbase, nconf, basis, seed)
@@ -270,10 +273,10 @@ def run(nbase=20, nconf=100, holdout=10, basis='syn-def2-svp', epochs=40, seed=0
 if __name__ == '__main__':
     import argparse
     ap = argparse.ArgumentParser()
-    ap.add_argument('--bases', type=int, default=20)
-    ap.add_argument('--conformers', type=int, default=100)
+    ap.add_argument('--bases', type=int, default=10)
+    ap.add_argument('--conformers', type=int, default=60)
     ap.add_argument('--holdout', type=int, default=10)
-    ap.add_argument('--epochs', type=int, default=40)
+    ap.add_argument('--epochs', type=int, default=60)
     ap.add_argument('--basis', default='syn-def2-svp')
     ap.add_argument('--out', default=None)
     a = ap.parse_args()
