@@ -79,6 +79,9 @@ class GuessModel:
     def __init__(self, nblock, hidden=256, seed=0):
         self.nblock = nblock
         self.net = mlp.DenseMLP([NFEAT, hidden, hidden, hidden, nblock * nblock], seed=seed)
+        # zero output layer: the untrained model predicts no correction (SAD)
+        self.net.W[-1].zero_()
+        self.net.b[-1].zero_()
         self.mu = np.zeros(NFEAT)
         self.sd = np.ones(NFEAT)
 
