@@ -39,6 +39,8 @@ CONFIGS = {
                 workload='synthetic C10N3O5H12 (seed 0), syn-def2-tzvp, SAD density, tol 1e-13'),
     'c10': dict(formula={'C': 4, 'N': 1, 'O': 1, 'H': 4}, seed=0, basis='syn-def2-tzvp',
                 workload='synthetic C4NOH4 (seed 0), syn-def2-tzvp, SAD density, tol 1e-13'),
+    'c120': dict(formula={'C': 40, 'N': 8, 'O': 12, 'H': 60}, seed=0, basis='syn-def2-tzvp',
+                 workload='synthetic C40N8O12H60 (seed 0), syn-def2-tzvp, RHF to 1e-8 Ha'),
     'h2o': dict(atom='O 0 0 0.1174; H -0.757 0 -0.4696; H 0.757 0 -0.4696', basis='syn-cc-pvdz',
                 workload='H2O, syn-cc-pvdz, SAD density, tol 1e-13'),
 }
@@ -265,6 +267,34 @@ def run_batched(steps, warmup):
             'quartets_per_s_graph': nquart / t_graph, 'max_abs_diff_vs_loop': err}
 
 
+def run_scf(args):
+    """Full RHF to 1e-8 Ha with DIIS on one molecule: FP64 J/K vs mixed
+    J/K (split args.split), both from the SAD guess."""
+    import torch
+    from gpu4pyscf_gb300.scf import hf
+    mol = make_mol(args.config)
+    rows = []
+    for prec in ('fp64', 'mixed'):
+        mf = hf.RHF(mol)
+        mf.conv_tol = 1e-8
+        mf.max_cycle = 60
+        mf.precision = prec
+        mf.split_thresh = args.split
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        e = mf.kernel()
+        torch.cuda.synchronize()
+        rows.append({'precision': prec, 'e_tot': e, 'cycles': mf.cycles, 'converged': mf.converged,
+                     'wall_s': time.perf_counter() - t0})
+    line = {'metric': 'scf_seconds_to_1e-8', 'value': rows[1]['wall_s'], 'unit': 's', 'n_gpus': 1,
+            'higher_is_better': False, 'dtype': 'f64/mixed', 'data': 'synthetic',
+            'config': {'workload': CONFIGS[args.config]['workload'], 'nao_user': mol.nao, 'natm': mol.natm,
+                       'split': args.split, 'guess': 'SAD'},
+            'runs': rows, 'dE_mixed_vs_fp64': rows[1]['e_tot'] - rows[0]['e_tot'],
+            'speedup_mixed_vs_fp64': rows[0]['wall_s'] / rows[1]['wall_s']}
+    print(json.dumps(line))
+
+
 def run_gpu(args):
     import torch
     import torch.distributed as dist
@@ -479,9 +509,13 @@ def main():
     ap.add_argument('--ref-seconds', type=float, default=20.)
     ap.add_argument('--no-cpu', action='store_true')
     ap.add_argument('--no-batch', action='store_true')
+    ap.add_argument('--mode', default='jk', choices=['jk', 'scf'],
+                    help='jk: the J/K benchmark line; scf: full RHF of --config (e.g. c120)')
     args = ap.parse_args()
     if args.impl == 'reference':
         run_reference(args)
+    elif args.mode == 'scf':
+        run_scf(args)
     else:
         run_gpu(args)
 

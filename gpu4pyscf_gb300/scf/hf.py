@@ -207,6 +207,21 @@ class RHF:
         e2 = 0.5 * torch.sum(dm * vhf).item()
         return e1 + e2, e2
 
+    def project_density(self, dm):
+        """Nearest idempotent RHF density with the molecule's electron count:
+        the nocc natural orbitals of largest occupation of ``dm`` (eigenvectors
+        of X^T S D S X), each doubly occupied.  Turns a predicted density,
+        which is neither idempotent nor of exact trace, into one whose
+        orbital gradient the DIIS error vector measures."""
+        X = self._X
+        s1e = self.get_ovlp()
+        dm = torch.as_tensor(dm, device='cuda', dtype=torch.float64)
+        p = X.T @ s1e @ dm @ s1e @ X
+        w, u = torch.linalg.eigh(0.5 * (p + p.T))
+        nocc = self.mol.nelectron // 2
+        c = X @ u[:, -nocc:]
+        return 2. * c @ c.T
+
     def get_init_guess(self, mol=None, key=None):
         from . import guess
         key = (key or self.init_guess).lower()
@@ -216,7 +231,7 @@ class RHF:
         if key == 'learned':
             if self.guess_model is None:
                 raise ValueError("init_guess='learned' needs RHF.guess_model")
-            return torch.as_tensor(self.guess_model.predict_density(self.mol), device='cuda')
+            return self.project_density(self.guess_model.predict_density(self.mol))
         if key in ('1e', 'hcore', 'core'):
             h = self.get_hcore()
             e, c = self.eig(h)

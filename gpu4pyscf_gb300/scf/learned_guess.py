@@ -10,8 +10,12 @@ frame: element one-hots of A and B, distance and its decays, the
 displacement and its direction, an element-resolved radial environment of
 each atom (Gaussians at 6 radii per element) and a same-atom flag.  The
 predicted blocks are assembled (D[B, A] = D[A, B]^T, diagonal blocks
-symmetrised) into the starting density of the SCF; the SCF's first Fock
-build and diagonalisation turn it into an idempotent density.
+symmetrised) and projected onto the nearest idempotent density with the
+right electron count (``RHF.project_density``: its nocc strongest natural
+orbitals, doubly occupied), which starts the SCF.  Without the projection
+the DIIS error vector of the first Fock matrix, a commutator with a
+non-idempotent density, under-reports how far that Fock matrix is from
+self-consistency, and DIIS leans on it.
 
 Training data are converged FP64 densities produced by this engine's own
 RHF on seeded conformers (random displacements of seeded base molecules).
@@ -171,8 +175,10 @@ def converged_density(mol, dm0=None, conv_tol=1e-9, precision='fp64'):
 
 def generate(confsets, holdout, conv_tol=1e-8, log=None):
     """Converged densities of every conformer except the last ``holdout`` of
-    each base molecule (those are kept for evaluation)."""
+    each base molecule (those are kept for evaluation).  Each conformer
+    starts from the converged density of the one before it."""
     data = []
+    cycles = []
     t0 = time.perf_counter()
     for b, confs in enumerate(confsets):
         prev = None
@@ -180,8 +186,11 @@ def generate(confsets, holdout, conv_tol=1e-8, log=None):
             mf = converged_density(mol, dm0=prev, conv_tol=conv_tol)
             prev = mf.dm.cpu().numpy()
             data.append((mol, prev))
+            if c:
+                cycles.append(mf.cycles)
         if log:
             log('base %d: %d conformers, %.1f s' % (b, len(confs) - holdout, time.perf_counter() - t0))
+    generate.chained_cycles = float(np.mean(cycles)) if cycles else None
     return data
 
 
@@ -228,26 +237,54 @@ def train(data, nblock, epochs=40, batch=4096, lr=1e-3, seed=0, log=None):
     return model
 
 
-def evaluate(model, mols, conv_tol=1e-8):
+def evaluate(model, mols, conv_tol=1e-8, n_raw=None):
+    """SCF cycles to conv_tol and converged energy from the SAD guess and
+    from the learned guess (projected to the nearest idempotent density),
+    per held-out molecule; on the first ``n_raw`` molecules also from the
+    unprojected learned density.  rms_* are the RMS element errors of the
+    guesses against the density converged from SAD."""
     rows = []
-    for mol in mols:
+    for k, mol in enumerate(mols):
         a = hf.RHF(mol)
         a.conv_tol = conv_tol
         e_sad = a.kernel()
+        d_conv = a.dm
+        raw = model.predict_density(mol)
         b = hf.RHF(mol)
         b.conv_tol = conv_tol
-        e_ml = b.kernel(dm0=model.predict_density(mol))
-        rows.append({'natm': mol.natm, 'nao': mol.nao, 'cycles_sad': a.cycles, 'cycles_learned': b.cycles,
-                     'e_sad': e_sad, 'e_learned': e_ml, 'converged': bool(a.converged and b.converged)})
+        proj = b.project_density(raw)
+        e_ml = b.kernel(dm0=proj)
+        sad = torch.as_tensor(guess.sad_density(mol), device='cuda')
+        rms = lambda d: float(torch.sqrt(torch.mean((torch.as_tensor(d, device='cuda') - d_conv) ** 2)).item())
+        row = {'natm': mol.natm, 'nao': mol.nao, 'cycles_sad': a.cycles, 'cycles_learned': b.cycles,
+               'e_sad': e_sad, 'e_learned': e_ml, 'converged': bool(a.converged and b.converged),
+               'rms_sad': rms(sad), 'rms_learned_raw': rms(raw), 'rms_learned': rms(proj)}
+        if n_raw is None or k < n_raw:
+            c = hf.RHF(mol)
+            c.conv_tol = conv_tol
+            row['e_learned_raw'] = c.kernel(dm0=raw)
+            row['cycles_learned_raw'] = c.cycles
+        rows.append(row)
     cs = np.array([r['cycles_sad'] for r in rows])
     cl = np.array([r['cycles_learned'] for r in rows])
-    de = np.array([abs(r['e_learned'] - r['e_sad']) for r in rows])
-    return {'n': len(rows), 'mean_cycles_sad': float(cs.mean()), 'mean_cycles_learned': float(cl.mean()),
-            'cycle_reduction': float(1 - cl.mean() / cs.mean()), 'max_abs_dE': float(de.max()),
-            'all_converged': all(r['converged'] for r in rows), 'rows': rows}
+    de = np.array([r['e_learned'] - r['e_sad'] for r in rows])
+    res = {'n': len(rows), 'mean_cycles_sad': float(cs.mean()), 'mean_cycles_learned': float(cl.mean()),
+           'cycle_reduction': float(1 - cl.mean() / cs.mean()), 'max_abs_dE': float(np.abs(de).max()),
+           'n_dE_above_1e-7': int((np.abs(de) > 1e-7).sum()), 'min_dE': float(de.min()),
+           'all_converged': all(r['converged'] for r in rows),
+           'mean_rms_sad': float(np.mean([r['rms_sad'] for r in rows])),
+           'mean_rms_learned_raw': float(np.mean([r['rms_learned_raw'] for r in rows])),
+           'mean_rms_learned': float(np.mean([r['rms_learned'] for r in rows])), 'rows': rows}
+    raw_rows = [r for r in rows if 'cycles_learned_raw' in r]
+    if raw_rows:
+        res['raw'] = {'n': len(raw_rows),
+                      'mean_cycles_sad': float(np.mean([r['cycles_sad'] for r in raw_rows])),
+                      'mean_cycles_learned_raw': float(np.mean([r['cycles_learned_raw'] for r in raw_rows])),
+                      'max_abs_dE': float(max(abs(r['e_learned_raw'] - r['e_sad']) for r in raw_rows))}
+    return res
 
 
-def run(nbase=10, nconf=60, holdout=10, basis='syn-def2-svp', epochs=60, seed=0, out=None):
+def run(nbase=10, nconf=60, holdout=10, basis='syn-def2-svp', epochs=300, seed=0, out=None, lr=2e-3, n_raw=20):
     log = lambda m: print(m, flush=True)
     t0 = time.perf_counter()
     confsets = make_conformers(nbase, nconf, basis, seed)
@@ -255,15 +292,18 @@ def run(nbase=10, nconf=60, holdout=10, basis='syn-def2-svp', epochs=60, seed=0,
     data = generate(confsets, holdout, log=log)
     t_gen = time.perf_counter() - t0
     t1 = time.perf_counter()
-    model = train(data, nblock, epochs=epochs, seed=seed, log=log)
+    model = train(data, nblock, epochs=epochs, lr=lr, seed=seed, log=log)
     t_train = time.perf_counter() - t1
     held = [m for cs in confsets for m in cs[len(cs) - holdout:]]
     t2 = time.perf_counter()
-    res = evaluate(model, held)
+    # interleave the bases so that a prefix (n_raw) covers all of them
+    held = [held[(i % nbase) * holdout + i // nbase] for i in range(len(held))]
+    res = evaluate(model, held, n_raw=n_raw)
     res.update({'workload': '%d base molecules (8-20 heavy atoms, C/N/O/H) x %d conformers (sigma 0.05 A), %s; '
                             '%d held out' % (nbase, nconf, basis, len(held)),
                 'train_conformers': len(data), 'train_pairs': int(sum(m.natm * (m.natm + 1) // 2 for m, _ in data)),
                 'final_train_loss': model.loss_history[-1], 'first_train_loss': model.loss_history[0],
+                'chained_cycles': generate.chained_cycles, 'epochs': epochs, 'lr': lr,
                 'generate_s': t_gen, 'train_s': t_train, 'evaluate_s': time.perf_counter() - t2})
     if out:
         slim = dict(res)
@@ -279,9 +319,11 @@ if __name__ == '__main__':
     ap.add_argument('--bases', type=int, default=10)
     ap.add_argument('--conformers', type=int, default=60)
     ap.add_argument('--holdout', type=int, default=10)
-    ap.add_argument('--epochs', type=int, default=60)
+    ap.add_argument('--epochs', type=int, default=300)
+    ap.add_argument('--lr', type=float, default=2e-3)
+    ap.add_argument('--n-raw', type=int, default=20)
     ap.add_argument('--basis', default='syn-def2-svp')
     ap.add_argument('--out', default=None)
     a = ap.parse_args()
-    res, _ = run(a.bases, a.conformers, a.holdout, a.basis, a.epochs, out=a.out)
+    res, _ = run(a.bases, a.conformers, a.holdout, a.basis, a.epochs, out=a.out, lr=a.lr, n_raw=a.n_raw)
     print(json.dumps({k: v for k, v in res.items() if k != 'rows'}))

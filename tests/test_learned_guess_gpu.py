@@ -15,7 +15,7 @@ def test_learned_guess_small():
     model = lg.train(data, nblock, epochs=80, batch=1024)
     assert model.loss_history[-1] < 0.5 * model.loss_history[0]
     held = [m for cs in confsets for m in cs[-2:]]
-    res = lg.evaluate(model, held)
+    res = lg.evaluate(model, held, n_raw=0)
     assert res['all_converged']
     assert res['max_abs_dE'] < 1e-7
     assert res['mean_cycles_learned'] <= res['mean_cycles_sad'] + 1
