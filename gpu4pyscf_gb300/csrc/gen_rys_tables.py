@@ -12,6 +12,10 @@ Method (this project's own tables; nothing is taken from other code):
   Chebyshev points and the interpolant is re-expanded, in high precision, in
   monomials of x = T - centre (x in [-1, 1]), so the device evaluates 13
   Horner steps per function.
+* The FP32 quartets use a second table on the same intervals with degree
+  DEG_F = 8 (9 Chebyshev points), whose interpolation error (< 4e-9
+  relative) is below FP32 rounding; fewer coefficients mean fewer loads and
+  FMAs per root evaluation.
 * T >= T_asym(n): u_r = h_r^2 / T, w_r = W_r / sqrt(T), with h_r, W_r the
   positive nodes and weights of 2n-point Gauss-Hermite quadrature (the
   integral over [0, 1] extended to [0, inf)).  T_asym(n) = 40 + 6n is where
@@ -26,6 +30,7 @@ import multiprocessing as mp_proc
 
 NMAX = 9
 DEG = 13
+DEG_F = 8
 WIDTH = 2
 DPS = 80
 
@@ -79,13 +84,14 @@ def hermite(mp, m):
 
 
 def fit_interval(args):
-    """Monomial coefficients [DEG+1][2n] in x = T - centre on one interval."""
-    n, k = args
+    """Monomial coefficients [deg+1][2n] in x = T - centre on one interval."""
+    n, k = args[:2]
+    deg = args[2] if len(args) > 2 else DEG
     mp = _mp()
     a = mp.mpf(k * WIDTH)
     half = mp.mpf(WIDTH) / 2
     c = a + half
-    N = DEG + 1
+    N = deg + 1
     nodes = [mp.cos(mp.pi * (j + mp.mpf(1) / 2) / N) for j in range(N)]
     vals = []
     for x in nodes:
@@ -123,7 +129,8 @@ def fit_interval(args):
 
 def check_interval(args):
     """Max relative error of the double-precision table on one interval."""
-    n, k, coef = args
+    n, k, coef = args[:3]
+    deg = args[3] if len(args) > 3 else DEG
     mp = _mp()
     worst = 0.
     for frac in (0.07, 0.31, 0.5, 0.77, 0.96):
@@ -132,8 +139,8 @@ def check_interval(args):
         ref = [float(v) for v in u + w]
         x = T - (k * WIDTH + WIDTH / 2)
         for f in range(2 * n):
-            acc = coef[DEG][f]
-            for i in range(DEG - 1, -1, -1):
+            acc = coef[deg][f]
+            for i in range(deg - 1, -1, -1):
                 acc = acc * x + coef[i][f]
             worst = max(worst, abs(acc - ref[f]) / abs(ref[f]))
     return worst
@@ -147,9 +154,13 @@ def main():
         res = pool.map(fit_interval, jobs, chunksize=4)
         table = {(n, k): c for n, k, c in res}
         errs = pool.map(check_interval, [(n, k, table[(n, k)]) for n, k in jobs], chunksize=4)
-    worst = {}
-    for (n, k), e in zip(jobs, errs):
+        res_f = pool.map(fit_interval, [(n, k, DEG_F) for n, k in jobs], chunksize=4)
+        table_f = {(n, k): c for n, k, c in res_f}
+        errs_f = pool.map(check_interval, [(n, k, table_f[(n, k)], DEG_F) for n, k in jobs], chunksize=4)
+    worst, worst_f = {}, {}
+    for (n, k), e, ef in zip(jobs, errs, errs_f):
         worst[n] = max(worst.get(n, 0.), e)
+        worst_f[n] = max(worst_f.get(n, 0.), ef)
     lines = []
     lines.append('// Generated by gen_rys_tables.py -- do not edit.')
     lines.append('// Rys roots/weights: piecewise degree-%d polynomials in x = T - centre on' % DEG)
@@ -157,8 +168,12 @@ def main():
     lines.append('// Max relative error of the double table vs 80-digit reference, per n:')
     for n in range(1, NMAX + 1):
         lines.append('//   n=%d: %.2e' % (n, worst[n]))
+    lines.append('// FP32 table (degree %d): max relative interpolation error per n (coefficients then rounded to float):' % DEG_F)
+    for n in range(1, NMAX + 1):
+        lines.append('//   n=%d: %.2e' % (n, worst_f[n]))
     lines.append('#define RYS_NMAX %d' % NMAX)
     lines.append('#define RYS_DEG %d' % DEG)
+    lines.append('#define RYS_DEG_F %d' % DEG_F)
     lines.append('#define RYS_WIDTH %d' % WIDTH)
     nint = [0] + [t_asym(n) // WIDTH for n in range(1, NMAX + 1)]
     # offs[n] = first element of the block for n roots (offs[0] unused)
@@ -177,6 +192,20 @@ def main():
             for i in range(DEG + 1):
                 lines.append('  ' + ', '.join(float.hex(v) for v in c[i]) + ',')
     lines.append('};')
+    offs_f = [0, 0]
+    for n in range(1, NMAX):
+        offs_f.append(offs_f[-1] + nint[n] * (DEG_F + 1) * 2 * n)
+    total_f = offs_f[-1] + nint[NMAX] * (DEG_F + 1) * 2 * NMAX
+    lines.append('#define RYS_TABLE_F_SIZE %d' % total_f)
+    lines.append('static const int rys_offset_f_host[RYS_NMAX + 1] = {%s};' % ', '.join(map(str, offs_f)))
+    lines.append('// FP32 layout per n: [interval][power 0..DEG_F][u_1..u_n, w_1..w_n]')
+    lines.append('static const float rys_coef_f_host[RYS_TABLE_F_SIZE] = {')
+    for n in range(1, NMAX + 1):
+        for k in range(nint[n]):
+            c = table_f[(n, k)]
+            for i in range(DEG_F + 1):
+                lines.append('  ' + ', '.join('%.9ef' % v for v in c[i]) + ',')
+    lines.append('};')
     hx, hw = [], []
     for n in range(1, NMAX + 1):
         x, W = hermite(mp, 2 * n)
@@ -191,7 +220,7 @@ def main():
     out = os.path.join(os.path.dirname(os.path.abspath(__file__)), 'rys_tables.inc')
     with open(out, 'w') as f:
         f.write('\n'.join(lines) + '\n')
-    print('wrote', out, 'max rel err', max(worst.values()))
+    print('wrote', out, 'max rel err', max(worst.values()), 'fp32 table', max(worst_f.values()))
 
 
 if __name__ == '__main__':

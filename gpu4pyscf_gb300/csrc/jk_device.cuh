@@ -42,6 +42,7 @@ struct PairList {
     const int2 *ij;        // shell indices (i >= j)
     const float *logq;     // log sqrt(max |(ij|ij)|)
     const int *prim_off;   // first primitive pair
+    const int *prim_cnt;   // primitive pairs kept for the pair
 };
 
 struct EngineDev {
@@ -75,6 +76,11 @@ struct EngineDev {
     int with_j, with_k;
     float log_cut;
     int fp32_asym;            // 1: FP32 quartets take the large-T asymptote in FP32 too
+    // range separation: omega2 = omega^2 > 0 evaluates erf(omega r)/r instead
+    // of 1/r (rys_roots_rs); op_scale multiplies every integral (a negative
+    // scale subtracts a long-range pass from a full-range one)
+    double omega2, op_scale;
+    float omega2_f, op_scale_f;
 };
 
 // Work of one quartet class.  The ket list is split into buckets of equal

@@ -280,6 +280,7 @@ struct HostPairList {
     std::vector<int2> ij;
     std::vector<float> logq;
     std::vector<int> prim_off;
+    std::vector<int> prim_cnt;
 };
 
 struct jk_opt {
@@ -302,6 +303,7 @@ struct jk_opt {
     int2 *pl_ij[NPAIRCLASS] = {nullptr};
     float *pl_logq[NPAIRCLASS] = {nullptr};
     int *pl_prim[NPAIRCLASS] = {nullptr};
+    int *pl_cnt[NPAIRCLASS] = {nullptr};     // primitive pairs kept per pair
     int nbk[NPAIRCLASS] = {0};           // ket buckets per molecule (max over molecules)
     int *pl_bstart[NPAIRCLASS] = {nullptr};  // bucket boundaries (molecule, primitive count)
     int *pl_mb0[NPAIRCLASS] = {nullptr};     // [nmol] first bucket of each molecule
@@ -329,7 +331,7 @@ struct jk_opt {
     double *dmj = nullptr, *dmk = nullptr, *jt = nullptr, *kt = nullptr;
     float *dmj_f = nullptr, *dmk_f = nullptr;
     unsigned long long *counters = nullptr;
-    int *work = nullptr;                 // [2 * NQCLASS] range counters of the class launches
+    int *work = nullptr;                 // [2 passes][NQCLASS][2 precisions] unit counters of the class launches
     std::vector<void *> owned;
     // side streams: class kernels of one build run concurrently on them,
     // forked from and joined back into the caller's stream with events
@@ -407,20 +409,51 @@ struct PrimPairHost {
     std::vector<double> ip;
 };
 
-void add_prim_pairs(const jk_opt *o, int i, int j, PrimPairHost &pp) {
+// Primitive pairs of shell pair (i, j).  With prune, pairs whose Gaussian
+// product is negligible, |K_ab| (pi/p)^(3/2) < 1e-18 (the overlap of the two
+// primitives; every integral of the pair is bounded by a small multiple of
+// it), are left out -- tight primitives on different atoms decay to nothing
+// -- but the largest one is always kept.  Returns the number added.
+constexpr double PRIM_PRUNE = 1e-18;
+
+inline double prim_weight(double a, double b, double ca, double cb, double AB2) {
+    double p = a + b;
+    return std::fabs(std::exp(-a * b / p * AB2) * ca * cb) * std::pow(M_PI / p, 1.5);
+}
+
+int add_prim_pairs(const jk_opt *o, int i, int j, PrimPairHost &pp, bool prune = false) {
     const ShellDev &A = o->shells_h[i], &B = o->shells_h[j];
     double AB2 = (A.x - B.x) * (A.x - B.x) + (A.y - B.y) * (A.y - B.y) + (A.z - B.z) * (A.z - B.z);
+    double wmax = 0.;
+    int kmax = 0;
+    if (prune) {
+        for (int pa = 0; pa < A.nprim; ++pa)
+            for (int pb = 0; pb < B.nprim; ++pb) {
+                double w = prim_weight(o->exps_h[o->prim0_h[i] + pa], o->exps_h[o->prim0_h[j] + pb],
+                                       o->coefs_h[o->prim0_h[i] + pa], o->coefs_h[o->prim0_h[j] + pb], AB2);
+                if (w > wmax) { wmax = w; kmax = pa * B.nprim + pb; }
+            }
+    }
+    int added = 0;
     for (int pa = 0; pa < A.nprim; ++pa)
         for (int pb = 0; pb < B.nprim; ++pb) {
             double a = o->exps_h[o->prim0_h[i] + pa], b = o->exps_h[o->prim0_h[j] + pb];
             double ca = o->coefs_h[o->prim0_h[i] + pa], cb = o->coefs_h[o->prim0_h[j] + pb];
+            if (prune && pa * B.nprim + pb != kmax && prim_weight(a, b, ca, cb, AB2) < PRIM_PRUNE) continue;
             double p = a + b;
             double K = std::exp(-a * b / p * AB2) * ca * cb;
             double Px = (a * A.x + b * B.x) / p, Py = (a * A.y + b * B.y) / p, Pz = (a * A.z + b * B.z) / p;
             pp.a.push_back(d4{p, Px, Py, Pz});
             pp.b.push_back(d4{Px - A.x, Py - A.y, Pz - A.z, K});
             pp.ip.push_back(1.0 / p);
+            ++added;
         }
+    return added;
+}
+
+int count_prim_pairs(const jk_opt *o, int i, int j) {
+    PrimPairHost tmp;
+    return add_prim_pairs(o, i, j, tmp, true);
 }
 
 int launch_class(const void *func, int grid, int smem, const EngineDev &d, const ClassDev &c, int ntiles,
@@ -452,6 +485,7 @@ EngineDev base_engine(const jk_opt *o) {
     d.nbas = o->nbas; d.nao = o->nao;
     d.ntot = o->ntot; d.mol_base = o->mol_base; d.mol_nao = o->mol_nao;
     d.mol_ndm = o->use_mol_ndm ? o->mol_ndm : nullptr;
+    d.op_scale = 1.; d.op_scale_f = 1.f;
     return d;
 }
 
@@ -631,7 +665,7 @@ static int create_impl(const int32_t *atm, int natm, const int32_t *bas, int nba
     if (int e = own_upload(o, &o->shells, o->shells_h)) return bail(e);
     {
         std::vector<double> t(rys_coef_host, rys_coef_host + RYS_TABLE_SIZE);
-        std::vector<float> tf(t.begin(), t.end());
+        std::vector<float> tf(rys_coef_f_host, rys_coef_f_host + RYS_TABLE_F_SIZE);
         if (int e = own_upload(o, &o->rys_coef, t)) return bail(e);
         if (int e = own_upload(o, &o->rys_coef_f, tf)) return bail(e);
     }
@@ -655,7 +689,7 @@ static int create_impl(const int32_t *atm, int natm, const int32_t *bas, int nba
             int pc = pair_class(A.l, B.l);
             cand[pc].ij.push_back(int2{i, j});
             cand[pc].prim_off.push_back((int)cpp.a.size());
-            add_prim_pairs(o, i, j, cpp);
+            cand[pc].prim_cnt.push_back(add_prim_pairs(o, i, j, cpp));
         }
     // Schwarz factors on the GPU
     {
@@ -666,6 +700,7 @@ static int create_impl(const int32_t *atm, int natm, const int32_t *bas, int nba
         if (int e = upload(&cip, cpp.ip)) { cudaFree(ca); cudaFree(cb); return bail(e); }
         std::vector<int2 *> dij(NPAIRCLASS, nullptr);
         std::vector<int *> dpo(NPAIRCLASS, nullptr);
+        std::vector<int *> dpc(NPAIRCLASS, nullptr);
         std::vector<float *> dq(NPAIRCLASS, nullptr);
         int err = 0;
         EngineDev d = base_engine(o);
@@ -675,6 +710,7 @@ static int create_impl(const int32_t *atm, int natm, const int32_t *bas, int nba
             if (n == 0) continue;
             if ((err = upload(&dij[pc], cand[pc].ij))) break;
             if ((err = upload(&dpo[pc], cand[pc].prim_off))) break;
+            if ((err = upload(&dpc[pc], cand[pc].prim_cnt))) break;
             if ((err = dalloc(&dq[pc], n))) break;
             const ClassEntry &e = g_tab[quartet_class(pc, pc)];
             ClassDev c;
@@ -682,6 +718,7 @@ static int create_impl(const int32_t *atm, int natm, const int32_t *bas, int nba
             c.bra.n = c.ket.n = n;
             c.bra.ij = c.ket.ij = dij[pc];
             c.bra.prim_off = c.ket.prim_off = dpo[pc];
+            c.bra.prim_cnt = c.ket.prim_cnt = dpc[pc];
             c.same = 1;
             c.class_id = quartet_class(pc, pc);
             d.qout = dq[pc];
@@ -699,7 +736,7 @@ static int create_impl(const int32_t *atm, int natm, const int32_t *bas, int nba
                 cudaMemcpy(qh[pc].data(), dq[pc], qh[pc].size() * sizeof(float), cudaMemcpyDeviceToHost) != cudaSuccess)
                 err = fail(JK_ERR_CUDA, "copy of Schwarz factors");
         }
-        for (int pc = 0; pc < NPAIRCLASS; ++pc) { cudaFree(dij[pc]); cudaFree(dpo[pc]); cudaFree(dq[pc]); }
+        for (int pc = 0; pc < NPAIRCLASS; ++pc) { cudaFree(dij[pc]); cudaFree(dpo[pc]); cudaFree(dpc[pc]); cudaFree(dq[pc]); }
         cudaFree(ca); cudaFree(cb); cudaFree(cip);
         if (err) return bail(err);
         // prune and sort
@@ -717,10 +754,9 @@ static int create_impl(const int32_t *atm, int natm, const int32_t *bas, int nba
                 o->qcond_h[(size_t)p.x * nbas + p.y] = o->qcond_h[(size_t)p.y * nbas + p.x] = qh[pc][k];
                 if (qh[pc][k] > 0 && qh[pc][k] >= keep) idx.push_back(k);
             }
-            auto npp = [&](int k) {
-                const int2 &p = cand[pc].ij[k];
-                return o->shells_h[p.x].nprim * o->shells_h[p.y].nprim;
-            };
+            std::vector<int> pruned(qh[pc].size(), 0);
+            for (int k : idx) pruned[k] = count_prim_pairs(o, cand[pc].ij[k].x, cand[pc].ij[k].y);
+            auto npp = [&](int k) { return pruned[k]; };
             auto molp = [&](int k) { return o->shells_h[cand[pc].ij[k].x].mol; };
             // order: molecule, primitive count (descending), Schwarz factor (descending)
             std::stable_sort(idx.begin(), idx.end(), [&](int a, int b) {
@@ -757,12 +793,13 @@ static int create_impl(const int32_t *atm, int natm, const int32_t *bas, int nba
                 fin.ij.push_back(p);
                 fin.logq.push_back(std::log(qh[pc][k]));
                 fin.prim_off.push_back((int)fpp.a.size());
-                add_prim_pairs(o, p.x, p.y, fpp);
+                fin.prim_cnt.push_back(add_prim_pairs(o, p.x, p.y, fpp, true));
             }
             o->npairs[pc] = (int)fin.ij.size();
             if (int e = own_upload(o, &o->pl_ij[pc], fin.ij)) return bail(e);
             if (int e = own_upload(o, &o->pl_logq[pc], fin.logq)) return bail(e);
             if (int e = own_upload(o, &o->pl_prim[pc], fin.prim_off)) return bail(e);
+            if (int e = own_upload(o, &o->pl_cnt[pc], fin.prim_cnt)) return bail(e);
         }
         std::vector<float4> af, bf;
         std::vector<float> ipf;
@@ -824,7 +861,7 @@ static int create_impl(const int32_t *atm, int natm, const int32_t *bas, int nba
     if (int e = own_alloc(o, &o->dm_cond, (size_t)nbas * nbas)) return bail(e);
     if (int e = own_alloc(o, &o->dm_max, 1)) return bail(e);
     if (int e = own_alloc(o, &o->counters, 4 * NQCLASS)) return bail(e);
-    if (int e = own_alloc(o, &o->work, 2 * NQCLASS)) return bail(e);
+    if (int e = own_alloc(o, &o->work, 4 * NQCLASS)) return bail(e);
     *out = o;
     return 0;
 }
@@ -862,8 +899,30 @@ static int ensure_workspace(jk_opt *o, int n_dm) {
     return 0;
 }
 
+// Operator passes of a build: lr * erf(|omega| r)/r + sr * erfc(|omega| r)/r
+// = sr * (1/r) + (lr - sr) * erf(|omega| r)/r, one pass per nonzero term.
+struct OpPass { double omega2, scale; };
+
+static int op_passes(double omega, double lr, double sr, OpPass *out) {
+    int n = 0;
+    if (omega == 0.) {
+        if (lr != sr) return -1;
+        out[n++] = OpPass{0., sr};
+        return n;
+    }
+    if (sr != 0.) out[n++] = OpPass{0., sr};
+    if (lr != sr) out[n++] = OpPass{omega * omega, lr - sr};
+    return n;
+}
+
 static int build_impl(jk_opt *o, const double *dm, int n_dm, int hermi, int with_j, int with_k, int precision,
-                      double split_thresh, double *vj, double *vk, void *stream, jk_stats *stats) {
+                      double split_thresh, double *vj, double *vk, void *stream, jk_stats *stats,
+                      double omega = 0., double lr_factor = 1., double sr_factor = 1.) {
+    OpPass passes[2];
+    const int npass = op_passes(omega, lr_factor, sr_factor, passes);
+    if (npass < 0 || !std::isfinite(omega) || !std::isfinite(lr_factor) || !std::isfinite(sr_factor))
+        return fail(JK_ERR_ARG, "jk_build: omega = 0 needs lr_factor == sr_factor");
+    if (npass == 0) return fail(JK_ERR_ARG, "jk_build: lr_factor = sr_factor = 0 gives no operator");
     if (!o || !dm || n_dm <= 0 || hermi < 0 || hermi > 2 || (!with_j && !with_k))
         return fail(JK_ERR_ARG, "jk_build: invalid arguments");
     if ((with_j && !vj) || (with_k && !vk)) return fail(JK_ERR_ARG, "jk_build: missing output buffer");
@@ -896,7 +955,7 @@ static int build_impl(jk_opt *o, const double *dm, int n_dm, int hermi, int with
     CK(cudaGetLastError());
     if (with_j) CK(cudaMemsetAsync(o->jt, 0, sizeof(double) * nn * n_dm, st));
     if (with_k) CK(cudaMemsetAsync(o->kt, 0, sizeof(double) * nn * n_dmk, st));
-    CK(cudaMemsetAsync(o->work, 0, sizeof(int) * 2 * NQCLASS, st));
+    CK(cudaMemsetAsync(o->work, 0, sizeof(int) * 4 * NQCLASS, st));
     const bool want_stats = stats != nullptr;
     if (want_stats) CK(cudaMemsetAsync(o->counters, 0, sizeof(unsigned long long) * 4 * NQCLASS, st));
 
@@ -911,7 +970,7 @@ static int build_impl(jk_opt *o, const double *dm, int n_dm, int hermi, int with
     d.fp32_asym = precision == JK_PREC_MIXED_FP32ROOTS;
     o->ev_slot.clear();
     if (o->time_classes) {
-        size_t need = 4 * o->plan_classes.size();
+        size_t need = 4 * o->plan_classes.size() * npass;
         while (o->ev.size() < need) {
             cudaEvent_t e;
             CK(cudaEventCreate(&e));
@@ -927,42 +986,47 @@ static int build_impl(jk_opt *o, const double *dm, int n_dm, int hermi, int with
         for (int i = 0; i < jk_opt::NSIDE; ++i) CK(cudaStreamWaitEvent(o->side[i], o->fork_ev, 0));
     }
     int nlaunched = 0;
-    for (auto it = o->plan_classes.rbegin(); it != o->plan_classes.rend(); ++it) {
-        const int q = *it;
-        const ClassEntry &e = g_tab[q];
-        int a = 0;
-        while ((a + 1) * (a + 2) / 2 <= q) ++a;
-        int b = q - a * (a + 1) / 2;
-        ClassDev c;
-        std::memset(&c, 0, sizeof(c));
-        c.bra = PairList{o->npairs[a], o->pl_ij[a], o->pl_logq[a], o->pl_prim[a]};
-        c.ket = PairList{o->npairs[b], o->pl_ij[b], o->pl_logq[b], o->pl_prim[b]};
-        c.same = a == b;
-        c.nbk = o->nbk[b];
-        c.nx = o->npairs[a] * o->nbk[b];
-        long long upper = (long long)o->npairs[a] * ((o->npairs[b] + e.qb64 - 1) / e.qb64 + o->nbk[b]);
-        if (!d.with_j && !d.with_k) break;
-        cudaStream_t ls = concurrent ? o->side[nlaunched++ % jk_opt::NSIDE] : st;
-        c.class_id = q;
-        d.counters = want_stats ? o->counters : nullptr;
-        c.work = o->work + 2 * q;
-        c.q_off = o->off64[q]; c.ket_begin = o->kb64[q]; c.ket_end = o->ke64[q];
-        if (o->time_classes) { o->ev_slot.push_back(2 * q); CK(cudaEventRecord(o->ev[2 * (o->ev_slot.size() - 1)], st)); }
-        if (int er = launch_variant(o, q, 0, upper, d, c, ls)) return er;
-        if (o->time_classes) CK(cudaEventRecord(o->ev[2 * (o->ev_slot.size() - 1) + 1], st));
-        ++launches;
-        if (mixed) {
-            c.class_id = NQCLASS + q;  // FP32 counters in the second half
-            c.work = o->work + 2 * q + 1;
-            c.q_off = o->off32[q]; c.ket_begin = o->kb32[q]; c.ket_end = o->ke32[q];
-            long long up32 = (long long)o->npairs[a] * ((o->npairs[b] + e.qb32 - 1) / e.qb32 + o->nbk[b]);
-            if (o->time_classes) { o->ev_slot.push_back(2 * q + 1); CK(cudaEventRecord(o->ev[2 * (o->ev_slot.size() - 1)], st)); }
-            cudaStream_t ls32 = concurrent ? o->side[nlaunched++ % jk_opt::NSIDE] : st;
-            if (int er = launch_variant(o, q, 1, up32, d, c, ls32)) return er;
+    for (int ip = 0; ip < npass; ++ip) {
+        d.omega2 = passes[ip].omega2; d.omega2_f = (float)passes[ip].omega2;
+        d.op_scale = passes[ip].scale; d.op_scale_f = (float)passes[ip].scale;
+        int *work = o->work + ip * 2 * NQCLASS;
+        for (auto it = o->plan_classes.rbegin(); it != o->plan_classes.rend(); ++it) {
+            const int q = *it;
+            const ClassEntry &e = g_tab[q];
+            int a = 0;
+            while ((a + 1) * (a + 2) / 2 <= q) ++a;
+            int b = q - a * (a + 1) / 2;
+            ClassDev c;
+            std::memset(&c, 0, sizeof(c));
+            c.bra = PairList{o->npairs[a], o->pl_ij[a], o->pl_logq[a], o->pl_prim[a], o->pl_cnt[a]};
+            c.ket = PairList{o->npairs[b], o->pl_ij[b], o->pl_logq[b], o->pl_prim[b], o->pl_cnt[b]};
+            c.same = a == b;
+            c.nbk = o->nbk[b];
+            c.nx = o->npairs[a] * o->nbk[b];
+            long long upper = (long long)o->npairs[a] * ((o->npairs[b] + e.qb64 - 1) / e.qb64 + o->nbk[b]);
+            if (!d.with_j && !d.with_k) break;
+            cudaStream_t ls = concurrent ? o->side[nlaunched++ % jk_opt::NSIDE] : st;
+            c.class_id = q;
+            d.counters = want_stats ? o->counters : nullptr;
+            c.work = work + 2 * q;
+            c.q_off = o->off64[q]; c.ket_begin = o->kb64[q]; c.ket_end = o->ke64[q];
+            if (o->time_classes) { o->ev_slot.push_back(2 * q); CK(cudaEventRecord(o->ev[2 * (o->ev_slot.size() - 1)], st)); }
+            if (int er = launch_variant(o, q, 0, upper, d, c, ls)) return er;
             if (o->time_classes) CK(cudaEventRecord(o->ev[2 * (o->ev_slot.size() - 1) + 1], st));
             ++launches;
+            if (mixed) {
+                c.class_id = NQCLASS + q;  // FP32 counters in the second half
+                c.work = work + 2 * q + 1;
+                c.q_off = o->off32[q]; c.ket_begin = o->kb32[q]; c.ket_end = o->ke32[q];
+                long long up32 = (long long)o->npairs[a] * ((o->npairs[b] + e.qb32 - 1) / e.qb32 + o->nbk[b]);
+                if (o->time_classes) { o->ev_slot.push_back(2 * q + 1); CK(cudaEventRecord(o->ev[2 * (o->ev_slot.size() - 1)], st)); }
+                cudaStream_t ls32 = concurrent ? o->side[nlaunched++ % jk_opt::NSIDE] : st;
+                if (int er = launch_variant(o, q, 1, up32, d, c, ls32)) return er;
+                if (o->time_classes) CK(cudaEventRecord(o->ev[2 * (o->ev_slot.size() - 1) + 1], st));
+                ++launches;
+            }
         }
-    }
+    }  // passes
     if (concurrent) {
         for (int i = 0; i < jk_opt::NSIDE; ++i) {
             CK(cudaEventRecord(o->join_ev[i], o->side[i]));
@@ -1009,6 +1073,14 @@ int jk_build(jk_opt *o, const double *dm, int n_dm, int nao, int hermi, int with
 int jk_build_batch(jk_opt *o, const double *dm, int n_dm, int hermi, int with_j, int with_k, int precision,
                    double split_thresh, double *vj, double *vk, void *stream, jk_stats *stats) {
     return build_impl(o, dm, n_dm, hermi, with_j, with_k, precision, split_thresh, vj, vk, stream, stats);
+}
+
+int jk_build_rsh(jk_opt *o, const double *dm, int n_dm, int nao, int hermi, int with_j, int with_k, double omega,
+                 double lr_factor, double sr_factor, int precision, double split_thresh, double *vj, double *vk,
+                 void *stream, jk_stats *stats) {
+    if (!o || o->nmol != 1 || nao != o->nao) return fail(JK_ERR_ARG, "jk_build_rsh: invalid arguments");
+    return build_impl(o, dm, n_dm, hermi, with_j, with_k, precision, split_thresh, vj, vk, stream, stats, omega,
+                      lr_factor, sr_factor);
 }
 
 long long jk_opt_ntot(const jk_opt *o) { return o ? o->ntot : -1; }
@@ -1079,8 +1151,8 @@ int jk_opt_tune(jk_opt *o, const double *dm, int n_dm, int hermi, int precision,
         const int b = q - a * (a + 1) / 2;
         ClassDev c;
         std::memset(&c, 0, sizeof(c));
-        c.bra = PairList{o->npairs[a], o->pl_ij[a], o->pl_logq[a], o->pl_prim[a]};
-        c.ket = PairList{o->npairs[b], o->pl_ij[b], o->pl_logq[b], o->pl_prim[b]};
+        c.bra = PairList{o->npairs[a], o->pl_ij[a], o->pl_logq[a], o->pl_prim[a], o->pl_cnt[a]};
+        c.ket = PairList{o->npairs[b], o->pl_ij[b], o->pl_logq[b], o->pl_prim[b], o->pl_cnt[b]};
         c.same = a == b;
         c.nbk = o->nbk[b];
         c.nx = o->npairs[a] * o->nbk[b];
@@ -1250,8 +1322,8 @@ extern "C" int jk_build_noalloc(jk_opt *o, const double *dm, int n_dm, int nao, 
             int bcls = q - a * (a + 1) / 2;
             ClassDev c;
             std::memset(&c, 0, sizeof(c));
-            c.bra = PairList{o->npairs[a], o->pl_ij[a], o->pl_logq[a], o->pl_prim[a]};
-            c.ket = PairList{o->npairs[bcls], o->pl_ij[bcls], o->pl_logq[bcls], o->pl_prim[bcls]};
+            c.bra = PairList{o->npairs[a], o->pl_ij[a], o->pl_logq[a], o->pl_prim[a], o->pl_cnt[a]};
+            c.ket = PairList{o->npairs[bcls], o->pl_ij[bcls], o->pl_logq[bcls], o->pl_prim[bcls], o->pl_cnt[bcls]};
             c.same = a == bcls;
             c.nbk = o->nbk[bcls];
             c.nx = o->npairs[a] * o->nbk[bcls];

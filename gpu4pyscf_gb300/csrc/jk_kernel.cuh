@@ -157,9 +157,9 @@ rys_class_kernel(EngineDev d, ClassDev c, int ntiles_static)
                     si.valid = 1;
                     si.ish = pij.x; si.jsh = pij.y; si.ksh = pkl.x; si.lsh = pkl.y;
                     si.pb_off = c.bra.prim_off[bra];
-                    si.npb = d.shells[pij.x].nprim * d.shells[pij.y].nprim;
+                    si.npb = c.bra.prim_cnt[bra];
                     si.pk_off = c.ket.prim_off[ket];
-                    si.npk = d.shells[pkl.x].nprim * d.shells[pkl.y].nprim;
+                    si.npk = c.ket.prim_cnt[ket];
                     si.nsteps = si.npb * si.npk;
                     float fac = 1.f;
                     if (pij.x == pij.y) fac *= .5f;
@@ -225,9 +225,9 @@ rys_class_kernel(EngineDev d, ClassDev c, int ntiles_static)
                     double ipq = rs * rs;
                     double PQx = a1.y - a2.y, PQy = a1.z - a2.z, PQz = a1.w - a2.w;
                     double T = p * q * ipq * (PQx * PQx + PQy * PQy + PQz * PQz);
-                    double pref = TWO_PI25 * b1.w * b2.w * ip1 * ip2 * rs;
+                    double pref = TWO_PI25 * b1.w * b2.w * ip1 * ip2 * rs * d.op_scale;
                     double u[NR], w[NR];
-                    rys_roots<NR>(T, d.rys_coef, u, w);
+                    rys_roots_rs<NR>(T, p * q * ipq, d.omega2, d.rys_coef, u, w);
 #pragma unroll
                     for (int r = 0; r < NR; ++r) { myrw[r] = (Real)u[r]; myrw[NR + r] = (Real)(w[r] * pref); }
                     m[0] = (Real)(0.5 * ip1); m[1] = (Real)(0.5 * ip2);
@@ -244,9 +244,9 @@ rys_class_kernel(EngineDev d, ClassDev c, int ntiles_static)
                     float ipq = rs * rs;
                     float PQx = a1.y - a2.y, PQy = a1.z - a2.z, PQz = a1.w - a2.w;
                     float T = p * q * ipq * (PQx * PQx + PQy * PQy + PQz * PQz);
-                    float pref = (float)TWO_PI25 * b1.w * b2.w * ip1 * ip2 * rs;
+                    float pref = (float)TWO_PI25 * b1.w * b2.w * ip1 * ip2 * rs * d.op_scale_f;
                     float u[NR], w[NR];
-                    rys_roots_f<NR>(T, d.rys_coef_f, u, w, d.fp32_asym);
+                    rys_roots_rs_f<NR>(T, p * q * ipq, d.omega2_f, d.rys_coef_f, u, w, d.fp32_asym);
 #pragma unroll
                     for (int r = 0; r < NR; ++r) { myrw[r] = (Real)u[r]; myrw[NR + r] = (Real)(w[r] * pref); }
                     m[0] = (Real)(0.5f * ip1); m[1] = (Real)(0.5f * ip2);

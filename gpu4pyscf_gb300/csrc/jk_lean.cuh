@@ -134,6 +134,15 @@ rys_lean_kernel(EngineDev d, ClassDev c, int unused)
     // quartets.
     __shared__ int2 queue[LEAN_THREADS / 32][64];
     __shared__ double aggbuf[LEAN_THREADS / 32][32];
+    // FP32: the Rys table block of this class in shared memory (the lanes'
+    // T values fall in different intervals; global loads of the table would
+    // cost one L1 wavefront per interval, shared loads one per instruction)
+    constexpr bool F32 = sizeof(Real) == 4;
+    __shared__ float s_rys[F32 ? rys_f_smem(NR) : 1];
+    if constexpr (F32) {
+        rys_stage_f<NR>(d.rys_coef_f, s_rys, threadIdx.x, blockDim.x);
+        __syncthreads();
+    }
     int2 *wq = queue[threadIdx.x >> 5];
     double *ab_buf = aggbuf[threadIdx.x >> 5];
     const int nunits = __ldg(c.q_off + c.nx);
@@ -187,14 +196,14 @@ rys_lean_kernel(EngineDev d, ClassDev c, int unused)
 #pragma unroll
         for (int e = 0; e < NF; ++e) acc[e] = Real(0);
         const ShellDev &A = d.shells[pij.x], &B = d.shells[pij.y];
-        const int npb = A.nprim * B.nprim;
+        const int npb = __ldg(c.bra.prim_cnt + ib);
         const int pb0 = c.bra.prim_off[ib];
         int npk = 0, pk0 = 0;
         Real abx = Real(A.x - B.x), aby = Real(A.y - B.y), abz = Real(A.z - B.z);
         Real cdx = 0, cdy = 0, cdz = 0;
         if (valid) {
             const ShellDev &C = d.shells[pkl.x], &D = d.shells[pkl.y];
-            npk = C.nprim * D.nprim;
+            npk = __ldg(c.ket.prim_cnt + ket);
             pk0 = c.ket.prim_off[ket];
             cdx = Real(C.x - D.x); cdy = Real(C.y - D.y); cdz = Real(C.z - D.z);
             if (d.counters) {
@@ -228,15 +237,18 @@ rys_lean_kernel(EngineDev d, ClassDev c, int unused)
                 const Real PQx = Px - Qx, PQy = Py - Qy, PQz = Pz - Qz;
                 if constexpr (sizeof(Real) == 8) {
                     rs = rsqrt(p + q);
-                    double T = p * q * rs * rs * (PQx * PQx + PQy * PQy + PQz * PQz);
-                    rys_roots<NR>(T, d.rys_coef, u, w);
+                    const double rho = p * q * rs * rs;
+                    double T = rho * (PQx * PQx + PQy * PQy + PQz * PQz);
+                    rys_roots_rs<NR>(T, rho, d.omega2, d.rys_coef, u, w);
                 } else {
                     rs = rsqrtf(p + q);
-                    float T = p * q * rs * rs * (PQx * PQx + PQy * PQy + PQz * PQz);
-                    rys_roots_f<NR>(T, d.rys_coef_f, u, w, d.fp32_asym);
+                    const float rho = p * q * rs * rs;
+                    float T = rho * (PQx * PQx + PQy * PQy + PQz * PQz);
+                    rys_roots_rs_f<NR, true>(T, rho, d.omega2_f, s_rys, u, w, d.fp32_asym);
                 }
                 const Real ipq = rs * rs;
-                const Real pref = Real(34.98683665524972497) * Kb * Kk * ipb * ipk * rs;
+                const Real pref = Real(34.98683665524972497) * Kb * Kk * ipb * ipk * rs *
+                                  (sizeof(Real) == 8 ? Real(d.op_scale) : Real(d.op_scale_f));
                 const Real qpq = q * ipq, ppq = p * ipq;
                 const Real h2p = Real(0.5) * ipb, h2q = Real(0.5) * ipk, h2pq = Real(0.5) * ipq;
 #pragma unroll

@@ -38,7 +38,8 @@ EXPORTS = ('jk_opt_create', 'jk_opt_destroy', 'jk_opt_nao', 'jk_opt_npairs',
            'jk_opt_get_qcond', 'jk_build', 'jk_last_error', 'jk_n_quartet_classes',
            'jk_opt_time_classes', 'jk_opt_class_times', 'jk_probe_fma', 'jk_int1e',
            'jk_int1e_last_error', 'jk_opt_create_batch', 'jk_build_batch', 'jk_opt_ntot',
-           'jk_opt_tune', 'jk_opt_set_variant', 'jk_opt_get_variant', 'jk_opt_set_mol_ndm')
+           'jk_opt_tune', 'jk_opt_set_variant', 'jk_opt_get_variant', 'jk_opt_set_mol_ndm',
+           'jk_build_rsh')
 
 
 def load(path=None):
@@ -86,6 +87,9 @@ def load(path=None):
         lib.jk_build_batch.argtypes = [vp, vp, i32, i32, i32, i32, i32, dp, vp, vp, vp,
                                        ctypes.POINTER(JKStats)]
         lib.jk_build_batch.restype = i32
+        lib.jk_build_rsh.argtypes = [vp, vp, i32, i32, i32, i32, i32, dp, dp, dp, i32, dp, vp, vp, vp,
+                                     ctypes.POINTER(JKStats)]
+        lib.jk_build_rsh.restype = i32
         lib.jk_opt_ntot.argtypes = [vp]
         lib.jk_opt_ntot.restype = ctypes.c_longlong
         lib.jk_opt_tune.argtypes = [vp, vp, i32, i32, i32, dp, vp, i32]

@@ -16,6 +16,7 @@ in, numpy out.
 
 import ctypes
 import math
+import sys
 import time
 
 import numpy as np
@@ -288,7 +289,9 @@ class RHF:
             g = f_mo[~occ][:, occ]
             gnorm = float(torch.linalg.norm(g).item()) * 2.
             if self.verbose:
-                print('cycle %d E=%.12f dE=%.3e |g|=%.3e' % (cycle + 1, e_tot, e_tot - e_last, gnorm))
+                print('cycle %d E=%.12f dE=%.3e |g|=%.3e  %.2f s' % (cycle + 1, e_tot, e_tot - e_last, gnorm,
+                                                                   time.perf_counter() - t0),
+                      file=sys.stderr, flush=True)
             if abs(e_tot - e_last) < self.conv_tol and gnorm < tol_grad:
                 self.converged = True
                 break

@@ -10,8 +10,13 @@ sm_103a kernels of libgb300jk.so; there is no CPU path.
 Differences from the reference, by design:
 * device arrays are torch CUDA tensors (the reference uses CuPy);
 * ``_VHFOpt.precision`` ('fp64', 'mixed' or 'mixed-fp32roots') and
-  ``_VHFOpt.split_thresh`` select the mixed FP32/FP64 evaluation;
-* range-separated operators (omega != 0) are not implemented and raise.
+  ``_VHFOpt.split_thresh`` select the mixed FP32/FP64 evaluation.
+
+Range separation follows the reference: J uses the operator of
+``mol.omega`` (libcint's convention, omega > 0 long range erf(omega r)/r,
+omega < 0 short range erfc(|omega| r)/r), K the operator
+lr_factor * erf(|omega| r)/r + sr_factor * erfc(|omega| r)/r resolved by
+``_check_rsh_factors`` (jk.py:1122-1168).
 """
 
 import ctypes
@@ -132,7 +137,9 @@ class _VHFOpt:
         return torch.matmul(self._coeff, mat)
 
     # -- J/K in the sorted basis --------------------------------------------
-    def _build(self, dms, hermi, with_j, with_k, stats=False):
+    def _build(self, dms, hermi, with_j, with_k, stats=False, op=(0., 1., 1.)):
+        """op = (omega >= 0, lr_factor, sr_factor) of the operator
+        lr * erf(omega r)/r + sr * erfc(omega r)/r; the default is 1/r."""
         if self.sorted_mol is None:
             self.build()
         dms = dms.contiguous()
@@ -143,15 +150,26 @@ class _VHFOpt:
         prec = libjk.PRECISIONS[self.precision]
         st = libjk.JKStats() if stats else None
         stream = torch.cuda.current_stream().cuda_stream
-        err = libjk.load().jk_build(self._handle, dms.data_ptr(), n_dm, nao, int(hermi),
-                                    int(with_j), int(with_k), prec, float(self.split_thresh),
-                                    vj.data_ptr() if with_j else None,
-                                    vk.data_ptr() if with_k else None,
-                                    stream, ctypes.byref(st) if stats else None)
-        libjk.check(err, 'jk_build')
+        lib = libjk.load()
+        omega, lr, sr = (float(x) for x in op)
+        out = (vj.data_ptr() if with_j else None, vk.data_ptr() if with_k else None)
+        if omega == 0. and lr == 1. and sr == 1.:
+            err = lib.jk_build(self._handle, dms.data_ptr(), n_dm, nao, int(hermi), int(with_j), int(with_k),
+                               prec, float(self.split_thresh), out[0], out[1], stream,
+                               ctypes.byref(st) if stats else None)
+            libjk.check(err, 'jk_build')
+        else:
+            err = lib.jk_build_rsh(self._handle, dms.data_ptr(), n_dm, nao, int(hermi), int(with_j), int(with_k),
+                                   abs(omega), lr, sr, prec, float(self.split_thresh), out[0], out[1], stream,
+                                   ctypes.byref(st) if stats else None)
+            libjk.check(err, 'jk_build_rsh')
         if stats:
             self.last_stats = st.as_dict()
         return vj, vk
+
+    def _mol_op(self):
+        """Operator of mol.omega (the basis environment's omega)."""
+        return _env_operator(getattr(self.mol, 'omega', 0.) or 0.)
 
     def tune(self, dm, hermi=1, reps=3):
         """Autotune each class's kernel family and grid on user-basis
@@ -170,23 +188,60 @@ class _VHFOpt:
                     'jk_opt_set_variant')
 
     def get_jk(self, dms, hermi, verbose=None, stats=False):
-        """J and K for densities in the sorted basis (jk.py:492-641)."""
-        return self._build(dms, hermi, True, True, stats)
+        """J and K for densities in the sorted basis (jk.py:492-641), both
+        with the operator of mol.omega."""
+        return self._build(dms, hermi, True, True, stats, op=self._mol_op())
 
     def get_j(self, dms, verbose=None):
-        return self._build(dms, 1, True, False)[0]
+        return self._build(dms, 1, True, False, op=self._mol_op())[0]
 
     def get_k(self, dms, hermi, verbose=None, omega=None, lr_factor=None, sr_factor=None):
-        if omega:
-            raise NotImplementedError('range-separated K (omega != 0) is not implemented')
-        return self._build(dms, hermi, False, True)[1]
+        """K with lr * erf(|omega| r)/r + sr * erfc(|omega| r)/r (jk.py:785-927)."""
+        omega, lr, sr = _check_rsh_factors(self.mol, omega, lr_factor, sr_factor)
+        op = self._mol_op() if omega == 0 else (abs(omega), lr, sr)
+        return self._build(dms, hermi, False, True, op=op)[1]
 
 
-def _check_omega(mol, omega):
+def _env_operator(omega):
+    """(|omega|, lr, sr) of libcint's sign convention for env omega."""
+    omega = float(omega)
+    if omega > 0:
+        return (omega, 1., 0.)
+    if omega < 0:
+        return (-omega, 0., 1.)
+    return (0., 1., 1.)
+
+
+def _check_rsh_factors(mol, omega, lr_factor, sr_factor):
+    """Resolve (omega, lr_factor, sr_factor) as gpu4pyscf/scf/jk.py:1122-1168
+    does: missing factors follow libcint's sign convention for omega, a
+    given pair with lr == sr means the full-range operator (omega -> 0), and
+    omega is returned negative whenever a short-range part is present."""
     if omega is None:
         omega = float(getattr(mol, 'omega', 0.) or 0.)
-    if omega != 0:
-        raise NotImplementedError('range-separated operators (omega != 0) are not implemented')
+    if lr_factor is None and sr_factor is None:
+        if omega == 0:
+            lr_factor = sr_factor = 1
+        elif omega < 0:
+            lr_factor, sr_factor = 0, 1
+        else:
+            lr_factor, sr_factor = 1, 0
+    elif lr_factor is None:
+        lr_factor = sr_factor if omega == 0 else 0
+    elif sr_factor is None:
+        if omega == 0:
+            sr_factor = lr_factor
+        else:
+            assert omega > 0
+            sr_factor = 0
+    else:
+        if omega == 0:
+            assert lr_factor == sr_factor
+        elif lr_factor == sr_factor:
+            omega = 0
+    if sr_factor != 0 and omega != 0:
+        omega = -abs(omega)
+    return omega, lr_factor, sr_factor
 
 
 def get_jk(mol, dm, hermi=0, vhfopt=None, with_j=True, with_k=True,
@@ -195,9 +250,11 @@ def get_jk(mol, dm, hermi=0, vhfopt=None, with_j=True, with_k=True,
 
     dm: (nao, nao) or (n, nao, nao), numpy or torch.  Returns (vj, vk) as
     torch CUDA tensors with the shape of dm; None for a skipped matrix.
+    J uses the operator of mol.omega; K uses
+    lr_factor * erf(|omega| r)/r + sr_factor * erfc(|omega| r)/r, the factors
+    resolved as in the reference (omega=None takes mol.omega).
     """
     assert with_j or with_k
-    _check_omega(mol, omega)
     if vhfopt is None:
         vhfopt = _VHFOpt(mol).build()
     dm = _as_device(dm)
@@ -205,7 +262,14 @@ def get_jk(mol, dm, hermi=0, vhfopt=None, with_j=True, with_k=True,
     nao = shape[-1]
     dms = dm.reshape(-1, nao, nao)
     dms = vhfopt.apply_coeff_C_mat_CT(dms)
-    vj, vk = vhfopt._build(dms, hermi, with_j, with_k)
+    omega, lr, sr = _check_rsh_factors(mol, omega, lr_factor, sr_factor)
+    op_j = _env_operator(getattr(mol, 'omega', 0.) or 0.)
+    op_k = op_j if omega == 0 else (abs(omega), lr, sr)
+    if op_j == op_k or not (with_j and with_k):
+        vj, vk = vhfopt._build(dms, hermi, with_j, with_k, op=op_j if with_j else op_k)
+    else:
+        vj = vhfopt._build(dms, hermi, True, False, op=op_j)[0]
+        vk = vhfopt._build(dms, hermi, False, True, op=op_k)[1]
     if with_j:
         vj = vhfopt.apply_coeff_CT_mat_C(vj).reshape(shape)
     if with_k:

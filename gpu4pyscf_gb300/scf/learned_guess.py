@@ -140,9 +140,12 @@ def base_formula(rng):
     return f
 
 
-def make_conformers(nbase, nconf, basis, seed=0, sigma=0.05):
-    """Seeded base molecules (8-20 heavy atoms) and nconf conformers each
-    (Gaussian displacements of sigma Angstrom); returns [[mol, ...], ...]."""
+def make_conformers(nbase, nconf, basis, seed=0, sigma=0.05, saturate=True):
+    """Seeded base molecules (8-20 heavy atoms; hydrogens on every free
+    valence unless saturate=False, which keeps the formula's H count and
+    gives open-valence, small-gap molecules with several SCF solutions) and
+    nconf conformers each (Gaussian displacements of sigma Angstrom);
+    returns [[mol, ...], ...]."""
     from ..gto import molgen
     rng = np.random.default_rng(seed)
     out = []
@@ -152,7 +155,7 @@ def make_conformers(nbase, nconf, basis, seed=0, sigma=0.05):
         s = 7919 * (b + 1) + seed
         for _ in range(50):
             try:
-                atoms = molgen.random_molecule(f, s)
+                atoms = molgen.random_molecule(f, s, saturate=saturate)
                 break
             except RuntimeError:
                 s += 1000003
@@ -299,8 +302,8 @@ def run(nbase=10, nconf=60, holdout=10, basis='syn-def2-svp', epochs=300, seed=0
     # interleave the bases so that a prefix (n_raw) covers all of them
     held = [held[(i % nbase) * holdout + i // nbase] for i in range(len(held))]
     res = evaluate(model, held, n_raw=n_raw)
-    res.update({'workload': '%d base molecules (8-20 heavy atoms, C/N/O/H) x %d conformers (sigma 0.05 A), %s; '
-                            '%d held out' % (nbase, nconf, basis, len(held)),
+    res.update({'workload': '%d base molecules (8-20 heavy atoms, C/N/O/H, H-saturated) x %d conformers '
+                            '(sigma 0.05 A), %s; %d held out' % (nbase, nconf, basis, len(held)),
                 'train_conformers': len(data), 'train_pairs': int(sum(m.natm * (m.natm + 1) // 2 for m, _ in data)),
                 'final_train_loss': model.loss_history[-1], 'first_train_loss': model.loss_history[0],
                 'chained_cycles': generate.chained_cycles, 'epochs': epochs, 'lr': lr,

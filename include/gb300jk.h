@@ -119,6 +119,23 @@ int jk_build_batch(jk_opt *opt, const double *dm, int n_dm, int hermi,
                    int with_j, int with_k, int precision, double split_thresh,
                    double *vj, double *vk, void *stream, jk_stats *stats);
 
+/* J/K with the range-separated operator
+ *     lr_factor * erf(|omega| r)/r + sr_factor * erfc(|omega| r)/r
+ * for both J and K; otherwise as jk_build.  Replaces the omega / lr_factor /
+ * sr_factor arguments of RYS_build_k (gpu4pyscf/lib/gvhf-rys/
+ * rys_contract_k.cu:605-612) and the omega that RYS_build_jk reads from the
+ * basis environment (env[8], libcint's PTR_RANGE_OMEGA), with the factor
+ * convention of gpu4pyscf/scf/jk.py:1122-1168 resolved by the caller:
+ * omega > 0 with (1, 0) is erf(omega r)/r, (0, 1) is erfc(|omega| r)/r.
+ * omega = 0 requires lr_factor == sr_factor (the Coulomb operator scaled).
+ * The short-range part is evaluated as full range minus long range (one
+ * extra pass of every class kernel); screening uses the full-range Schwarz
+ * factors, which bound both parts. */
+int jk_build_rsh(jk_opt *opt, const double *dm, int n_dm, int nao, int hermi,
+                 int with_j, int with_k, double omega, double lr_factor, double sr_factor,
+                 int precision, double split_thresh, double *vj, double *vk,
+                 void *stream, jk_stats *stats);
+
 /* Autotuner (no counterpart in the reference, whose launch schemes are
  * fixed per class).  jk_opt_tune times, for every angular class (and
  * precision) the optimizer launches, each kernel family the class has

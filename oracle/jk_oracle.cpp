@@ -20,6 +20,15 @@
 //
 // Inputs use the libcint layout (atm[natm][6], bas[nbas][8], env) in the
 // Cartesian AO basis of the given shells (nctr contractions per shell).
+//
+// Range separation follows libcint's convention (env[8] = omega, the slot
+// PySCF's mol.omega writes; gpu4pyscf/scf/jk.py:1122-1168): omega > 0 gives
+// the long-range operator erf(omega r)/r, omega < 0 the short-range
+// erfc(|omega| r)/r.  Writing 1/r = 2/sqrt(pi) int_0^inf exp(-s^2 r^2) ds,
+// the long-range operator stops the integral at s = omega; for a primitive
+// quartet with reduced exponent a = pq/(p+q) this turns the Hermite
+// integrals R_tuv(a) into sqrt(theta) R_tuv(theta a) with
+// theta = omega^2 / (omega^2 + a).  Short range = full - long range.
 
 #include <cmath>
 #include <cstdint>
@@ -34,6 +43,7 @@ namespace {
 
 constexpr int ATOM_OF = 0, ANG_OF = 1, NPRIM_OF = 2, NCTR_OF = 3, PTR_EXP = 5, PTR_COEFF = 6;
 constexpr int CHARGE_OF = 0, PTR_COORD = 1;
+constexpr int PTR_RANGE_OMEGA = 8;
 constexpr int LMAX = 7;
 
 inline int ncart(int l) { return (l + 1) * (l + 2) / 2; }
@@ -185,7 +195,8 @@ struct Rtab {
 // Contracted Cartesian ERI block (ij|kl), layout
 // out[(((ci*nctr_j + cj)*nctr_k + ck)*nctr_l + cl)][a][b][c][d]
 // with a,b,c,d running over Cartesian components.
-void eri_block(const Shell &si, const Shell &sj, const Shell &sk, const Shell &sl, std::vector<double> &out) {
+void eri_block(const Shell &si, const Shell &sj, const Shell &sk, const Shell &sl, std::vector<double> &out,
+               double omega = 0.0) {
     int la = si.l, lb = sj.l, lc = sk.l, ld = sl.l;
     int na = ncart(la), nb = ncart(lb), nc = ncart(lc), nd = ncart(ld);
     int nabcd = na * nb * nc * nd;
@@ -200,7 +211,7 @@ void eri_block(const Shell &si, const Shell &sj, const Shell &sk, const Shell &s
     double rab2 = AB[0] * AB[0] + AB[1] * AB[1] + AB[2] * AB[2];
     double rcd2 = CD[0] * CD[0] + CD[1] * CD[1] + CD[2] * CD[2];
     Eaxis Eab[3], Ecd[3];
-    Rtab R;
+    Rtab R, Rlr;
     int nh = lab + 1;  // bra Hermite index range per axis
     std::vector<double> W((size_t)nh * nh * nh);
     std::vector<double> prim(nabcd);
@@ -222,7 +233,17 @@ void eri_block(const Shell &si, const Shell &sj, const Shell &sk, const Shell &s
             for (int x = 0; x < 3; ++x) Ecd[x].build(lc, ld, q, Q[x] - sk.r[x], Q[x] - sl.r[x]);
             double alpha = p * q / (p + q);
             double pref = 2.0 * std::pow(M_PI, 2.5) / (p * q * std::sqrt(p + q)) * Kab * Kcd;
-            R.build(L, alpha, P[0] - Q[0], P[1] - Q[1], P[2] - Q[2], pref);
+            if (omega > 0) {
+                double theta = omega * omega / (omega * omega + alpha);
+                R.build(L, alpha * theta, P[0] - Q[0], P[1] - Q[1], P[2] - Q[2], pref * std::sqrt(theta));
+            } else {
+                R.build(L, alpha, P[0] - Q[0], P[1] - Q[1], P[2] - Q[2], pref);
+                if (omega < 0) {
+                    double theta = omega * omega / (omega * omega + alpha);
+                    Rlr.build(L, alpha * theta, P[0] - Q[0], P[1] - Q[1], P[2] - Q[2], pref * std::sqrt(theta));
+                    for (size_t e = 0; e < R.cur.size(); ++e) R.cur[e] -= Rlr.cur[e];
+                }
+            }
             for (int ic = 0; ic < nc; ++ic)
             for (int id = 0; id < nd; ++id) {
                 // W_tuv = sum_{tau,nu,phi} (-1)^(tau+nu+phi) Ecd R_{t+tau,u+nu,v+phi}
@@ -307,7 +328,7 @@ int oracle_eri_full(const int *atm, int natm, const int *bas, int nbas, const do
     for (int j = 0; j < nbas; ++j)
     for (int k = 0; k < nbas; ++k)
     for (int l = 0; l < nbas; ++l) {
-        eri_block(sh[i], sh[j], sh[k], sh[l], blk);
+        eri_block(sh[i], sh[j], sh[k], sh[l], blk, env[PTR_RANGE_OMEGA]);
         int na = ncart(sh[i].l), nb = ncart(sh[j].l), nc = ncart(sh[k].l), nd = ncart(sh[l].l);
         for (int ci = 0; ci < sh[i].nctr; ++ci)
         for (int cj = 0; cj < sh[j].nctr; ++cj)
@@ -337,7 +358,7 @@ int oracle_qcond(const int *atm, int natm, const int *bas, int nbas, const doubl
         int i = ij / nbas, j = ij % nbas;
         if (j > i) continue;
         std::vector<double> blk;
-        eri_block(sh[i], sh[j], sh[i], sh[j], blk);
+        eri_block(sh[i], sh[j], sh[i], sh[j], blk, env[PTR_RANGE_OMEGA]);
         int na = ncart(sh[i].l) , nb = ncart(sh[j].l);
         int nctr = sh[i].nctr * sh[j].nctr;
         double m = 0.0;
@@ -421,7 +442,7 @@ int oracle_jk(const int *atm, int natm, const int *bas, int nbas, const double *
                     }
                     ++n_comp;
                     n_prim += (long long)sh[i].nprim * sh[j].nprim * sh[k].nprim * sh[l].nprim;
-                    eri_block(sh[i], sh[j], sh[k], sh[l], blk);
+                    eri_block(sh[i], sh[j], sh[k], sh[l], blk, env[PTR_RANGE_OMEGA]);
                     double fac = 1.0;
                     if (i == j) fac *= 0.5;
                     if (k == l) fac *= 0.5;
