@@ -267,6 +267,39 @@ def run_batched(steps, warmup):
             'quartets_per_s_graph': nquart / t_graph, 'max_abs_diff_vs_loop': err}
 
 
+def nvtx_push(name):
+    try:
+        import torch
+        torch.cuda.nvtx.range_push(name)
+    except Exception:
+        pass
+
+
+def nvtx_pop():
+    try:
+        import torch
+        torch.cuda.nvtx.range_pop()
+    except Exception:
+        pass
+
+
+def kernel_family(li, lj, lk, ll):
+    """Kernel family the engine launches by default for a class: the
+    register-resident kernel when the Cartesian ERI block plus one root's
+    2D integrals fit in 64 registers' worth of values (LEAN_MAX in
+    csrc/jk_classes.cu), else the block-cooperative one."""
+    nc = lambda l: (l + 1) * (l + 2) // 2
+    nf = nc(li) * nc(lj) * nc(lk) * nc(ll)
+    gs = (li + 1) * (lj + 1) * (lk + 1) * (ll + 1)
+    return 'rys_lean_kernel' if nf + 3 * gs <= 64 else 'rys_class_kernel'
+
+
+# DRAM bytes (read + write) per launch of class kernels from one ncu capture
+# of the default command (profiles/ summaries of the same name give the
+# capture); the roofline's traffic when the dominant class is among them
+NCU_DRAM_BYTES = {}
+
+
 def run_scf(args):
     """Full RHF to 1e-8 Ha with DIIS on one molecule: FP64 J/K vs mixed
     J/K (split args.split), both from the SAD guess."""
@@ -280,6 +313,8 @@ def run_scf(args):
         mf.max_cycle = 60
         mf.precision = prec
         mf.split_thresh = args.split
+        mf.verbose = True          # per-cycle progress on stderr
+        print('== %s' % prec, file=sys.stderr, flush=True)
         torch.cuda.synchronize()
         t0 = time.perf_counter()
         e = mf.kernel()
@@ -340,7 +375,11 @@ def run_gpu(args):
         dist.barrier()
     clocks = ClockSampler()
     clocks.start()
+    # NVTX range: lets a profiler select the timed builds' launches
+    # (ncu --nvtx --nvtx-include 'jk_timed/')
+    nvtx_push('jk_timed')
     t64 = timed(build64, args.steps)
+    nvtx_pop()
     clock_info = clocks.stop()
     tmax = torch.tensor([sum(t64)], dtype=torch.float64, device='cuda')
     if world > 1:
@@ -357,7 +396,9 @@ def run_gpu(args):
 
     def mixed_eval(split, prec, steps):
         opt.precision, opt.split_thresh = prec, split
+        nvtx_push('jk_mixed_%g_%s' % (split, prec))
         opt._build(dms, 1, True, True, stats=True)
+        nvtx_pop()
         st = dict(opt.last_stats)
         fn = lambda: opt._build(dms, 1, True, True)
         for _ in range(2):
@@ -436,9 +477,11 @@ def run_gpu(args):
            'share_of_build': float(best_ms[k] / max(best_ms[0::2].sum(), 1e-12))}
     achieved = fl[k] / (best_ms[k] * 1e-3) / 1e12 if best_ms[k] > 0 else 0.
     total_fp64_tflops = st64['flops_fp64'] / t_step / 1e12
+    lk4 = tuple(int(L[i][k // 2]) for i in range(4))
+    traffic = NCU_DRAM_BYTES.get((args.config, dom['class']))
     roofline = {'bound': 'fp64', 'achieved': achieved, 'peak': peak64 / 1e12, 'unit': 'TFLOP/s',
-                'frac': achieved / (peak64 / 1e12), 'traffic': None,
-                'kernel': 'rys_class_kernel %s FP64' % dom['class'], 'dominant': dom,
+                'frac': achieved / (peak64 / 1e12), 'traffic': traffic,
+                'kernel': '%s %s FP64' % (kernel_family(*lk4), dom['class']), 'dominant': dom,
                 'peak_source': 'FP64 FMA-chain probe measured in this run (MEASURED_PEAKS.json has no FP64 figure)',
                 'fp32_peak_tflops': peak32 / 1e12,
                 'whole_build_fp64_tflops': total_fp64_tflops,

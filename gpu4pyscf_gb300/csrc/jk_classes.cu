@@ -11,38 +11,43 @@
 
 namespace jk {
 
-// classes whose ERI block plus 2D integrals fit in registers take the
-// register-resident kernel
+// classes whose ERI block plus one root's 2D integrals fit in registers take
+// the register-resident kernel: up to 64 values in FP64, and up to 130 in
+// FP32, about the same number of 32-bit registers
 constexpr int LEAN_MAX = 64;
+constexpr int LEAN_MAX_F32 = 130;
 
 template <int LI, int LJ, int LK, int LL>
 static void reg_one(ClassEntry *tab) {
     using S64 = ClassShape<LI, LJ, LK, LL, double>;
     using S32 = ClassShape<LI, LJ, LK, LL, float>;
+    constexpr int COST = LeanShape<LI, LJ, LK, LL>::COST;
     ClassEntry &e = tab[quartet_class(pair_class(LI, LJ), pair_class(LK, LL))];
     e.li = LI; e.lj = LJ; e.lk = LK; e.ll = LL;
-    e.qb64 = S64::QB; e.smem64 = S64::SMEM;
-    e.qb32 = S32::QB; e.smem32 = S32::SMEM;
-    if constexpr (LeanShape<LI, LJ, LK, LL>::COST <= LEAN_MAX) {
-        e.lean = 1;
+    e.threads_alt = JK_THREADS;
+    if constexpr (COST <= LEAN_MAX) {
+        e.lean64 = 1;
         e.k64 = (const void *)rys_lean_kernel<LI, LJ, LK, LL, double>;
-        e.k32 = (const void *)rys_lean_kernel<LI, LJ, LK, LL, float>;
-        e.qb64 = e.qb32 = LEAN_THREADS;
-        e.smem64 = e.smem32 = 0;
-        e.threads64 = e.threads32 = LEAN_THREADS;
+        e.qb64 = LEAN_THREADS; e.smem64 = 0; e.threads64 = LEAN_THREADS;
         e.k64_alt = (const void *)rys_class_kernel<LI, LJ, LK, LL, double, MODE_JK>;
-        e.k32_alt = (const void *)rys_class_kernel<LI, LJ, LK, LL, float, MODE_JK>;
         e.smem64_alt = S64::SMEM;
-        e.smem32_alt = S32::SMEM;
-        e.threads_alt = JK_THREADS;
     } else {
-        e.k64_alt = e.k32_alt = nullptr;
-        e.smem64_alt = e.smem32_alt = 0;
-        e.threads_alt = 0;
-        e.lean = 0;
+        e.lean64 = 0;
         e.k64 = (const void *)rys_class_kernel<LI, LJ, LK, LL, double, MODE_JK>;
+        e.qb64 = S64::QB; e.smem64 = S64::SMEM; e.threads64 = JK_THREADS;
+        e.k64_alt = nullptr; e.smem64_alt = 0;
+    }
+    if constexpr (COST <= LEAN_MAX_F32) {
+        e.lean32 = 1;
+        e.k32 = (const void *)rys_lean_kernel<LI, LJ, LK, LL, float>;
+        e.qb32 = LEAN_THREADS; e.smem32 = 0; e.threads32 = LEAN_THREADS;
+        e.k32_alt = (const void *)rys_class_kernel<LI, LJ, LK, LL, float, MODE_JK>;
+        e.smem32_alt = S32::SMEM;
+    } else {
+        e.lean32 = 0;
         e.k32 = (const void *)rys_class_kernel<LI, LJ, LK, LL, float, MODE_JK>;
-        e.threads64 = e.threads32 = JK_THREADS;
+        e.qb32 = S32::QB; e.smem32 = S32::SMEM; e.threads32 = JK_THREADS;
+        e.k32_alt = nullptr; e.smem32_alt = 0;
     }
     if constexpr (LI == LK && LJ == LL) {
         e.kdiag = (const void *)rys_class_kernel<LI, LJ, LK, LL, double, MODE_DIAG>;

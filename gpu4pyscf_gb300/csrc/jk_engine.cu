@@ -466,8 +466,8 @@ int launch_class(const void *func, int grid, int smem, const EngineDev &d, const
 int set_smem_attrs() {
     for (int q = 0; q < NQCLASS; ++q) {
         const ClassEntry &e = g_tab[q];
-        if (e.k64 && !e.lean) CK(cudaFuncSetAttribute(e.k64, cudaFuncAttributeMaxDynamicSharedMemorySize, e.smem64));
-        if (e.k32 && !e.lean) CK(cudaFuncSetAttribute(e.k32, cudaFuncAttributeMaxDynamicSharedMemorySize, e.smem32));
+        if (e.k64 && !e.lean64) CK(cudaFuncSetAttribute(e.k64, cudaFuncAttributeMaxDynamicSharedMemorySize, e.smem64));
+        if (e.k32 && !e.lean32) CK(cudaFuncSetAttribute(e.k32, cudaFuncAttributeMaxDynamicSharedMemorySize, e.smem32));
         if (e.kdiag) CK(cudaFuncSetAttribute(e.kdiag, cudaFuncAttributeMaxDynamicSharedMemorySize, e.smemdiag));
         if (e.k64_alt) CK(cudaFuncSetAttribute(e.k64_alt, cudaFuncAttributeMaxDynamicSharedMemorySize, e.smem64_alt));
         if (e.k32_alt) CK(cudaFuncSetAttribute(e.k32_alt, cudaFuncAttributeMaxDynamicSharedMemorySize, e.smem32_alt));
@@ -503,11 +503,11 @@ int grid_for(const jk_opt *o, long long upper_tiles, int lean = 0) {
 int launch_variant(const jk_opt *o, int q, int prec, long long upper, const EngineDev &d, const ClassDev &c,
                    cudaStream_t st) {
     const ClassEntry &e = g_tab[q];
-    const int alt = o->variant_alt[2 * q + prec] && e.k64_alt;
+    const int alt = o->variant_alt[2 * q + prec] && (prec ? e.k32_alt : e.k64_alt);
     const void *k = prec ? (alt ? e.k32_alt : e.k32) : (alt ? e.k64_alt : e.k64);
     const int smem = prec ? (alt ? e.smem32_alt : e.smem32) : (alt ? e.smem64_alt : e.smem64);
     const int threads = alt ? e.threads_alt : (prec ? e.threads32 : e.threads64);
-    const int lean = alt ? 0 : e.lean;
+    const int lean = alt ? 0 : (prec ? e.lean32 : e.lean64);
     int grid;
     if (o->variant_grid[2 * q + prec] > 0)
         grid = (int)std::max<long long>(1, std::min<long long>(upper, (long long)o->sm_count * o->variant_grid[2 * q + prec]));
@@ -1165,7 +1165,7 @@ int jk_opt_tune(jk_opt *o, const double *dm, int n_dm, int hermi, int precision,
             c.ket_end = prec ? o->ke32[q] : o->ke64[q];
             float best = 1e30f;
             int best_alt = 0, best_grid = 0;
-            for (int alt = 0; alt <= (e.k64_alt ? 1 : 0) && !err; ++alt)
+            for (int alt = 0; alt <= ((prec ? e.k32_alt : e.k64_alt) ? 1 : 0) && !err; ++alt)
                 for (int gi = 0; gi < 4 && !err; ++gi) {
                     o->variant_alt[2 * q + prec] = alt;
                     o->variant_grid[2 * q + prec] = grids[gi];
@@ -1331,13 +1331,13 @@ extern "C" int jk_build_noalloc(jk_opt *o, const double *dm, int n_dm, int nao, 
             c.work = work + 2 * q;
             c.q_off = o->off64[q]; c.ket_begin = o->kb64[q]; c.ket_end = o->ke64[q];
             long long upper = (long long)o->npairs[a] * ((o->npairs[bcls] + e.qb64 - 1) / e.qb64 + o->nbk[bcls]);
-            if (int er = launch_class(e.k64, grid_for(o, upper, e.lean), e.smem64, d, c, 0, st, e.threads64)) return er;
+            if (int er = launch_class(e.k64, grid_for(o, upper, e.lean64), e.smem64, d, c, 0, st, e.threads64)) return er;
             if (mixed) {
                 c.class_id = NQCLASS + q;
                 c.work = work + 2 * q + 1;
                 c.q_off = o->off32[q]; c.ket_begin = o->kb32[q]; c.ket_end = o->ke32[q];
                 long long up32 = (long long)o->npairs[a] * ((o->npairs[bcls] + e.qb32 - 1) / e.qb32 + o->nbk[bcls]);
-                if (int er = launch_class(e.k32, grid_for(o, up32, e.lean), e.smem32, d, c, 0, st, e.threads32)) return er;
+                if (int er = launch_class(e.k32, grid_for(o, up32, e.lean32), e.smem32, d, c, 0, st, e.threads32)) return er;
             }
         }
     }

@@ -93,19 +93,23 @@ __device__ __forceinline__ void rys2d(Real i00, Real c00, Real cp00, Real b00, R
 
 // Atomic add aggregated over the lanes of a warp that target the same
 // address: one atomic per distinct address (lanes with addr == nullptr add
-// nothing).  All 32 lanes must call it together.
-__device__ __forceinline__ void warp_agg_add(double *addr, double v, double *buf, int lane) {
+// nothing).  The lanes' values are summed in the kernel's precision (for the
+// FP32 quartets a sum of at most 32 FP32 integrals, within their own error)
+// and converted once for the FP64 accumulator.  All 32 lanes must call it
+// together.
+template <typename Real>
+__device__ __forceinline__ void warp_agg_add(double *addr, Real v, Real *buf, int lane) {
     const unsigned peers = __match_any_sync(0xffffffffu, (unsigned long long)addr);
     buf[lane] = v;
     __syncwarp();
     if (addr != nullptr && lane == __ffs(peers) - 1) {
-        double s = 0.;
+        Real s = Real(0);
         unsigned m = peers;
         while (m) {
             s += buf[__ffs(m) - 1];
             m &= m - 1;
         }
-        if (s != 0.) atomicAdd(addr, s);
+        if (s != Real(0)) atomicAdd(addr, (double)s);
     }
     __syncwarp();
 }
@@ -133,7 +137,7 @@ rys_lean_kernel(EngineDev d, ClassDev c, int unused)
     // a time and queues the quartets that pass; each iteration runs 32 queued
     // quartets.
     __shared__ int2 queue[LEAN_THREADS / 32][64];
-    __shared__ double aggbuf[LEAN_THREADS / 32][32];
+    __shared__ Real aggbuf[LEAN_THREADS / 32][32];
     // FP32: the Rys table block of this class in shared memory (the lanes'
     // T values fall in different intervals; global loads of the table would
     // cost one L1 wavefront per interval, shared loads one per instruction)
@@ -144,7 +148,7 @@ rys_lean_kernel(EngineDev d, ClassDev c, int unused)
         __syncthreads();
     }
     int2 *wq = queue[threadIdx.x >> 5];
-    double *ab_buf = aggbuf[threadIdx.x >> 5];
+    Real *ab_buf = aggbuf[threadIdx.x >> 5];
     const int nunits = __ldg(c.q_off + c.nx);
     int kcur = 0, kend = 0, bcur = 0;
     bool exhausted = false;
@@ -313,14 +317,16 @@ rys_lean_kernel(EngineDev d, ClassDev c, int unused)
                     Real s = Real(0);
 #pragma unroll
                     for (int cd = 0; cd < NFK * NFL; ++cd) s += acc[ab * NFK * NFL + cd] * dkl[cd];
-                    double sd = vd ? (double)(fac * s) : 0.;
+                    // (summed across the warp in the kernel's precision,
+                    // converted once for the FP64 accumulator)
+                    Real sd = vd ? fac * s : Real(0);
                     double *dst = V + (size_t)(ai + ab / NFJ) * nao + aj + ab % NFJ;
                     if (same_bra) {
 #pragma unroll
                         for (int off = 16; off > 0; off >>= 1) sd += __shfl_xor_sync(0xffffffffu, sd, off);
-                        if (lane == 0 && sd != 0.) atomicAdd(dst, sd);
+                        if (lane == 0 && sd != Real(0)) atomicAdd(dst, (double)sd);
                     } else if (vd) {
-                        atomicAdd(dst, sd);
+                        atomicAdd(dst, (double)sd);
                     }
                 }
                 if (vd) {
@@ -366,7 +372,7 @@ rys_lean_kernel(EngineDev d, ClassDev c, int unused)
                         for (int b = 0; b < NFJ; ++b)
 #pragma unroll
                             for (int dd = 0; dd < NFL; ++dd) s += acc[((a * NFJ + b) * NFK + cc) * NFL + dd] * djl[b * NFL + dd];
-                        warp_agg_add(vd ? V + (size_t)(ai + a) * nao + ak + cc : nullptr, (double)(fac * s), ab_buf, lane);
+                        warp_agg_add(vd ? V + (size_t)(ai + a) * nao + ak + cc : nullptr, fac * s, ab_buf, lane);
                     }
 #pragma unroll
                 for (int a = 0; a < NFI; ++a)
@@ -377,7 +383,7 @@ rys_lean_kernel(EngineDev d, ClassDev c, int unused)
                         for (int b = 0; b < NFJ; ++b)
 #pragma unroll
                             for (int cc = 0; cc < NFK; ++cc) s += acc[((a * NFJ + b) * NFK + cc) * NFL + dd] * djk[b * NFK + cc];
-                        warp_agg_add(vd ? V + (size_t)(ai + a) * nao + al + dd : nullptr, (double)(fac * s), ab_buf, lane);
+                        warp_agg_add(vd ? V + (size_t)(ai + a) * nao + al + dd : nullptr, fac * s, ab_buf, lane);
                     }
 #pragma unroll
                 for (int b = 0; b < NFJ; ++b)
@@ -388,7 +394,7 @@ rys_lean_kernel(EngineDev d, ClassDev c, int unused)
                         for (int a = 0; a < NFI; ++a)
 #pragma unroll
                             for (int dd = 0; dd < NFL; ++dd) s += acc[((a * NFJ + b) * NFK + cc) * NFL + dd] * dil[a * NFL + dd];
-                        warp_agg_add(vd ? V + (size_t)(aj + b) * nao + ak + cc : nullptr, (double)(fac * s), ab_buf, lane);
+                        warp_agg_add(vd ? V + (size_t)(aj + b) * nao + ak + cc : nullptr, fac * s, ab_buf, lane);
                     }
 #pragma unroll
                 for (int b = 0; b < NFJ; ++b)
@@ -399,7 +405,7 @@ rys_lean_kernel(EngineDev d, ClassDev c, int unused)
                         for (int a = 0; a < NFI; ++a)
 #pragma unroll
                             for (int cc = 0; cc < NFK; ++cc) s += acc[((a * NFJ + b) * NFK + cc) * NFL + dd] * dik[a * NFK + cc];
-                        warp_agg_add(vd ? V + (size_t)(aj + b) * nao + al + dd : nullptr, (double)(fac * s), ab_buf, lane);
+                        warp_agg_add(vd ? V + (size_t)(aj + b) * nao + al + dd : nullptr, fac * s, ab_buf, lane);
                     }
             }
         }

@@ -16,12 +16,13 @@ struct ClassEntry {
     int li, lj, lk, ll;
     int qb64, smem64, qb32, smem32, qbdiag, smemdiag;
     int threads64, threads32;   // block size of the J/K kernels
-    int lean;                   // 1: register-resident kernel, 0: block-cooperative
+    int lean64, lean32;         // 1: register-resident kernel, 0: block-cooperative
     const void *k64;     // FP64 J/K kernel
     const void *k32;     // FP32 J/K kernel
     const void *kdiag;   // Schwarz kernel (bra class == ket class only)
     // alternative kernel family for the autotuner (block-cooperative kernel of
-    // a class that defaults to the register-resident one; null otherwise)
+    // a class and precision that default to the register-resident one; null
+    // otherwise)
     const void *k64_alt;
     const void *k32_alt;
     int smem64_alt, smem32_alt, threads_alt;
