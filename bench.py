@@ -294,10 +294,11 @@ def kernel_family(li, lj, lk, ll):
     return 'rys_lean_kernel' if nf + 3 * gs <= 64 else 'rys_class_kernel'
 
 
-# DRAM bytes (read + write) per launch of class kernels from one ncu capture
-# of the default command (profiles/ summaries of the same name give the
-# capture); the roofline's traffic when the dominant class is among them
-NCU_DRAM_BYTES = {}
+# DRAM bytes (read + write) per launch of FP64 class kernels of the timed
+# build, from one ncu capture of the c30 command (--set full, one launch of
+# the class inside the 'jk_timed' NVTX range); the roofline's traffic when
+# the dominant class is among them
+NCU_DRAM_BYTES = {('c30', '(21|11)'): 3100160, ('c30', '(11|10)'): 3365376}
 
 
 def run_scf(args):
