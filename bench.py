@@ -267,6 +267,22 @@ def run_batched(steps, warmup):
             'quartets_per_s_graph': nquart / t_graph, 'max_abs_diff_vs_loop': err}
 
 
+def max_over_ranks(seconds, world, device):
+    """The slowest rank's timed-region seconds (all ranks must call it)."""
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([float(seconds)], dtype=torch.float64, device=device)
+    if world > 1:
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def job_rate(units_per_rank, world, seconds_per_step):
+    """Whole-job rate of N replicas (weak scaling: every rank does the same
+    build): all ranks' units over the slowest rank's time."""
+    return units_per_rank * world / seconds_per_step
+
+
 def nvtx_push(name):
     try:
         import torch
@@ -382,11 +398,8 @@ def run_gpu(args):
     t64 = timed(build64, args.steps)
     nvtx_pop()
     clock_info = clocks.stop()
-    tmax = torch.tensor([sum(t64)], dtype=torch.float64, device='cuda')
-    if world > 1:
-        dist.all_reduce(tmax, op=dist.ReduceOp.MAX)
-    t_step = float(tmax.item()) / args.steps
-    value = st64['quartets_fp64'] * world / t_step
+    t_step = max_over_ranks(sum(t64), world, 'cuda') / args.steps
+    value = job_rate(st64['quartets_fp64'], world, t_step)
 
     # reference results for the error of the mixed build
     vj64, vk64 = opt._build(dms, 1, True, True)
@@ -507,8 +520,10 @@ def run_gpu(args):
 
     for _ in range(args.warmup):
         e2e()
+    if world > 1:
+        dist.barrier()
     te = timed(e2e, args.steps)
-    e2e_val = st64['quartets_fp64'] * world / (sum(te) / args.steps)
+    e2e_val = job_rate(st64['quartets_fp64'], world, max_over_ranks(sum(te), world, 'cuda') / args.steps)
     nbytes = dm_host.numel() * 8
 
     batched = None
