@@ -347,6 +347,49 @@ def run_scf(args):
     print(json.dumps(line))
 
 
+def run_dense(args):
+    """J/K of a dense SCF density (the density after the first SCF step from
+    SAD, what every later Fock build of an SCF sees), FP64 against mixed at
+    splits 1e-6 and 1e-4: seconds per build, speed-up, max |dJ|, |dK| and the
+    two-electron energy change.  The SAD density of the default benchmark is
+    block diagonal by atom, which the density screening exploits; this is the
+    build of the SCF iterations."""
+    import torch
+    from gpu4pyscf_gb300.scf import hf, jk
+    mol = make_mol(args.config)
+    mf = hf.RHF(mol)
+    dm0 = mf.get_init_guess()
+    f = mf.get_hcore() + mf.get_veff(None, dm0)
+    e, c = mf.eig(f)
+    dm = mf.make_rdm1(c, mf.get_occ(e, c))
+    opt = mf.opt
+    rows = []
+    ref = None
+    for prec, split in (('fp64', 1e-6), ('mixed', 1e-6), ('mixed', 1e-4)):
+        opt.precision, opt.split_thresh = prec, split
+        jk.get_jk(mol, dm, 1, opt)          # warm-up (plans, workspace)
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        vj, vk = jk.get_jk(mol, dm, 1, opt)
+        e1.record()
+        torch.cuda.synchronize()
+        t = e0.elapsed_time(e1) * 1e-3
+        if ref is None:
+            ref = (vj, vk, t)
+        de = 0.5 * float(torch.sum(dm * (vj - ref[0]))) - 0.25 * float(torch.sum(dm * (vk - ref[1])))
+        rows.append({'precision': prec, 'split': split if prec != 'fp64' else None, 's_per_jk_build': t,
+                     'speedup_vs_fp64': ref[2] / t, 'max_abs_dJ': float((vj - ref[0]).abs().max()),
+                     'max_abs_dK': float((vk - ref[1]).abs().max()), 'dE_2e_Ha': de})
+        print(json.dumps(rows[-1]), file=sys.stderr, flush=True)
+    line = {'metric': 'jk_build_seconds_dense_density', 'value': rows[-1]['s_per_jk_build'], 'unit': 's',
+            'n_gpus': 1, 'higher_is_better': False, 'dtype': 'f64/mixed', 'data': 'synthetic',
+            'config': {'workload': CONFIGS[args.config]['workload'], 'nao_user': mol.nao, 'natm': mol.natm,
+                       'density': 'first SCF step from SAD (dense)'},
+            'runs': rows}
+    print(json.dumps(line))
+
+
 def run_gpu(args):
     import torch
     import torch.distributed as dist
@@ -568,13 +611,16 @@ def main():
     ap.add_argument('--ref-seconds', type=float, default=20.)
     ap.add_argument('--no-cpu', action='store_true')
     ap.add_argument('--no-batch', action='store_true')
-    ap.add_argument('--mode', default='jk', choices=['jk', 'scf'],
-                    help='jk: the J/K benchmark line; scf: full RHF of --config (e.g. c120)')
+    ap.add_argument('--mode', default='jk', choices=['jk', 'scf', 'dense'],
+                    help='jk: the J/K benchmark line; scf: full RHF of --config (e.g. c120); '
+                         'dense: FP64 vs mixed J/K of a dense SCF density of --config')
     args = ap.parse_args()
     if args.impl == 'reference':
         run_reference(args)
     elif args.mode == 'scf':
         run_scf(args)
+    elif args.mode == 'dense':
+        run_dense(args)
     else:
         run_gpu(args)
 
