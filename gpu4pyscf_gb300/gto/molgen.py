@@ -35,8 +35,10 @@ def _saturate(symbols, coords, free, rng, ndir=4096, bond=(1.0, 1.1), d_heavy=1.
     valences first.  The hydrogens of one heavy atom are placed together:
     among ndir random sets of directions (X-H bond lengths from U(1.0, 1.1)
     A) the set farthest from every other atom and from each other is kept;
-    it needs 1.8 A to other heavy atoms, 1.45 A to the heavy atoms bonded to
-    its own and 1.6 A between hydrogens (geminal H-H in CH4 is 1.78 A)."""
+    it needs 1.8 A to other heavy atoms and 1.6 A to other hydrogens
+    (geminal H-H in CH4 is 1.78 A), except 1.45 A to any atom within 1.6 A
+    of its own heavy atom (the heavy atoms bonded to it and their
+    hydrogens)."""
     symbols, coords = list(symbols), [np.asarray(c) for c in coords]
     nheavy = len(symbols)
     for parent in sorted(range(nheavy), key=lambda k: -free[k]):
@@ -48,9 +50,9 @@ def _saturate(symbols, coords, free, rng, ndir=4096, bond=(1.0, 1.1), d_heavy=1.
         pos = coords[parent] + dirs * rng.uniform(*bond, size=(ndir, m, 1))
         idx = [k for k in range(len(coords)) if k != parent]
         others = np.array([coords[k] for k in idx])
-        # atoms bonded to the parent (within 1.6 A) are 1-3 neighbours of
-        # its hydrogens: with heavy-atom bonds as short as 1.0 A they need
-        # a smaller clearance
+        # atoms within 1.6 A of the parent (its bonded heavy atoms and their
+        # hydrogens) are 1-3 neighbours of its hydrogens: with heavy-atom
+        # bonds as short as 1.0 A they need a smaller clearance
         near = np.linalg.norm(others - coords[parent], axis=-1) < 1.6
         lim = np.where(near, d_13, np.array([d_h if symbols[k] == 'H' else d_heavy for k in idx]))
         margin = (np.linalg.norm(pos[:, :, None, :] - others[None, None], axis=-1) - lim).min(axis=(1, 2))
