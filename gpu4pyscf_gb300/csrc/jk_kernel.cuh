@@ -1,6 +1,5 @@
 // Per-class Rys J/K kernel template (see jk_device.cuh for the scheme).
 #pragma once
-#include "f32_to_f64.h"
 #include "jk_device.cuh"
 #include "rys_roots.cuh"
 
@@ -450,8 +449,7 @@ rys_class_kernel(EngineDev d, ClassDev c, int ntiles_static)
                         out = V + (size_t)(aj + b) * nao + al + dd;
                     }
                 }
-                if constexpr (sizeof(Real) == 8) atomicAdd(out, (double)si.fac * (double)sum);
-                else atomicAdd(out, f32_to_f64_exact(si.fac * (float)sum));
+                atomicAdd(out, (double)si.fac * (double)sum);
             }
         }
         __syncthreads();

@@ -12,7 +12,6 @@
 // shuffles before one atomic add per element; the four K blocks go out with
 // one atomic add per distinct address of the warp, J_kl directly.
 #pragma once
-#include "f32_to_f64.h"
 #include "jk_device.cuh"
 #include "rys_roots.cuh"
 
@@ -92,10 +91,6 @@ __device__ __forceinline__ void rys2d(Real i00, Real c00, Real cp00, Real b00, R
         }
 }
 
-// Widening for the FP64 accumulators: FP32 values through the integer pipe
-__device__ __forceinline__ double to_f64(double v) { return v; }
-__device__ __forceinline__ double to_f64(float v) { return f32_to_f64_exact(v); }
-
 // Atomic add aggregated over the lanes of a warp that target the same
 // address: one atomic per distinct address (lanes with addr == nullptr add
 // nothing).  The lanes' values are summed in the kernel's precision (for the
@@ -114,7 +109,7 @@ __device__ __forceinline__ void warp_agg_add(double *addr, Real v, Real *buf, in
             s += buf[__ffs(m) - 1];
             m &= m - 1;
         }
-        if (s != Real(0)) atomicAdd(addr, to_f64(s));
+        if (s != Real(0)) atomicAdd(addr, (double)s);
     }
     __syncwarp();
 }
@@ -295,10 +290,8 @@ rys_lean_kernel(EngineDev d, ClassDev c, int unused)
         const size_t nn = (size_t)d.ntot;
         const size_t mbase = (size_t)__ldg(d.mol_base + mol);
         const int ndm_m = d.mol_ndm ? __ldg(d.mol_ndm + mol) : d.n_dm;
-        Real fac = Real(1);
-        if (pij.x == pij.y) fac *= Real(0.5);
-        if (pkl.x == pkl.y) fac *= Real(0.5);
-        if (c.same && ib == ket) fac *= Real(0.5);
+        const Real fac = Real((pij.x == pij.y ? .5 : 1.) * (pkl.x == pkl.y ? .5 : 1.) *
+                              (c.same && ib == ket ? .5 : 1.));
         const int ai = A.ao, aj = B.ao;
         const int ak = valid ? d.shells[pkl.x].ao : 0, al = valid ? d.shells[pkl.y].ao : 0;
         if (d.with_j) {
@@ -331,9 +324,9 @@ rys_lean_kernel(EngineDev d, ClassDev c, int unused)
                     if (same_bra) {
 #pragma unroll
                         for (int off = 16; off > 0; off >>= 1) sd += __shfl_xor_sync(0xffffffffu, sd, off);
-                        if (lane == 0 && sd != Real(0)) atomicAdd(dst, to_f64(sd));
+                        if (lane == 0 && sd != Real(0)) atomicAdd(dst, (double)sd);
                     } else if (vd) {
-                        atomicAdd(dst, to_f64(sd));
+                        atomicAdd(dst, (double)sd);
                     }
                 }
                 if (vd) {
@@ -342,7 +335,7 @@ rys_lean_kernel(EngineDev d, ClassDev c, int unused)
                         Real s = Real(0);
 #pragma unroll
                         for (int ab = 0; ab < NFI * NFJ; ++ab) s += acc[ab * NFK * NFL + cd] * dij[ab];
-                        atomicAdd(V + (size_t)(ak + cd / NFL) * nao + al + cd % NFL, to_f64(fac * s));
+                        atomicAdd(V + (size_t)(ak + cd / NFL) * nao + al + cd % NFL, (double)(fac * s));
                     }
                 }
             }
