@@ -12,13 +12,19 @@ Printed JSON line (one per run, rank 0):
               pinned host memory, host->device copy, basis transforms, build,
               device->host copy of J and K inside the timed region);
   mixed       the mixed FP32/FP64 build at split 1e-6: quartets/s, speed-up
-              over FP64 and the error against the FP64 build;
+              over FP64 and the error against the FP64 build, and a sweep
+              of splits 1e-8 .. 1e-2;
+  mixed_dense FP64 vs mixed (splits 1e-6, 1e-4) for a dense SCF density of
+              the same molecule (the first SCF step from SAD);
   roofline    the dominant class kernel: algorithmic FP64 FLOP/s against the
               FP64 FMA peak measured here by an FMA-chain probe;
   cpu_baseline  the C++ CPU oracle on this host's cores on a bounded sample.
 
 --impl reference runs the CPU implementation of the path (the oracle, the
 restatement of PySCF's get_jk) on all host cores for the same workload.
+--mode scf runs a full RHF of --config (FP64 and mixed J/K); --mode dense
+times FP64 against mixed J/K on a dense SCF density of --config (c120: the
+120-atom molecule).
 """
 import argparse
 import ctypes
@@ -347,16 +353,16 @@ def run_scf(args):
     print(json.dumps(line))
 
 
-def run_dense(args):
-    """J/K of a dense SCF density (the density after the first SCF step from
-    SAD, what every later Fock build of an SCF sees), FP64 against mixed at
-    splits 1e-6 and 1e-4: seconds per build, speed-up, max |dJ|, |dK| and the
-    two-electron energy change.  The SAD density of the default benchmark is
-    block diagonal by atom, which the density screening exploits; this is the
-    build of the SCF iterations."""
+def dense_mixed(mol, splits=(1e-6, 1e-4)):
+    """J/K of a dense SCF density of mol (the density after the first SCF
+    step from SAD, what every later Fock build of an SCF sees), FP64 against
+    mixed at the given splits: seconds per build (CUDA events, after one
+    warm-up build each), speed-up, max |dJ|, |dK| and the two-electron energy
+    change.  The SAD density of the default benchmark is block diagonal by
+    atom, which the density screening exploits; this is the build of the SCF
+    iterations."""
     import torch
     from gpu4pyscf_gb300.scf import hf, jk
-    mol = make_mol(args.config)
     mf = hf.RHF(mol)
     dm0 = mf.get_init_guess()
     f = mf.get_hcore() + mf.get_veff(None, dm0)
@@ -365,7 +371,7 @@ def run_dense(args):
     opt = mf.opt
     rows = []
     ref = None
-    for prec, split in (('fp64', 1e-6), ('mixed', 1e-6), ('mixed', 1e-4)):
+    for prec, split in [('fp64', splits[0])] + [('mixed', x) for x in splits]:
         opt.precision, opt.split_thresh = prec, split
         jk.get_jk(mol, dm, 1, opt)          # warm-up (plans, workspace)
         torch.cuda.synchronize()
@@ -382,6 +388,14 @@ def run_dense(args):
                      'speedup_vs_fp64': ref[2] / t, 'max_abs_dJ': float((vj - ref[0]).abs().max()),
                      'max_abs_dK': float((vk - ref[1]).abs().max()), 'dE_2e_Ha': de})
         print(json.dumps(rows[-1]), file=sys.stderr, flush=True)
+    opt.precision = 'fp64'
+    return rows
+
+
+def run_dense(args):
+    """bench.py --mode dense: dense_mixed on --config, one JSON line."""
+    mol = make_mol(args.config)
+    rows = dense_mixed(mol)
     line = {'metric': 'jk_build_seconds_dense_density', 'value': rows[-1]['s_per_jk_build'], 'unit': 's',
             'n_gpus': 1, 'higher_is_better': False, 'dtype': 'f64/mixed', 'data': 'synthetic',
             'config': {'workload': CONFIGS[args.config]['workload'], 'nao_user': mol.nao, 'natm': mol.natm,
@@ -573,6 +587,13 @@ def run_gpu(args):
     if not args.no_batch:
         batched = run_batched(2, 1)
 
+    # mixed precision on the density an SCF iteration sees (dense), next to
+    # the SAD-density numbers above; reported, never fatal to the line
+    try:
+        mixed_dense = {'density': 'first SCF step from SAD (dense)', 'runs': dense_mixed(mol)}
+    except Exception as exc:  # noqa: BLE001
+        mixed_dense = {'error': '%s: %s' % (type(exc).__name__, exc)}
+
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu:
         cpu = cpu_sample(mol, dm, target_s=args.cpu_seconds)
@@ -592,7 +613,7 @@ def run_gpu(args):
                 'e2e': {'value': e2e_val, 'unit': 'quartets/s', 'h2d_bytes_per_step': nbytes,
                         'd2h_bytes_per_step': 2 * nbytes, 's_per_step': sum(te) / args.steps},
                 'gpu_launches': int(st64['kernel_launches']) * args.steps,
-                'mixed': mixed, 'roofline': roofline, 'classes_top': per_class[:8],
+                'mixed': mixed, 'mixed_dense': mixed_dense, 'roofline': roofline, 'classes_top': per_class[:8],
                 'batched': batched, 'cpu_baseline': cpu, 'clocks': clock_info}
         print(json.dumps(line))
     if world > 1:
