@@ -264,13 +264,38 @@ def run_batched(steps, warmup):
     out = b.replay()
     torch.cuda.synchronize()
     err = max(float(abs(a - r).max().item()) for a, r in zip(out[0] + out[1], [x[0] for x in ref] + [x[1] for x in ref]))
+    # the whole batch in mixed precision (one launch per class and precision,
+    # tuned FP64 launches), against the FP64 batch: seconds, speed-up over the
+    # tuned FP64 batch, max elementwise error, max |dE_2e| over the densities
+    mixed = {}
+    try:
+        j0, k0 = b.get_jk(dms_dev)
+        for split in (1e-6, 1e-4):
+            b.precision, b.split_thresh = 'mixed', split
+            for _ in range(warmup):
+                eager()
+            t_m = timed_wall(eager, steps)
+            jm, km = b.get_jk(dms_dev)
+            e_max = max(float(abs(a - r).max().item()) for a, r in zip(jm + km, j0 + k0))
+            de = 0.
+            for d, a, a0, c, c0 in zip(dms_dev, jm, j0, km, k0):
+                d3 = d if d.ndim == 3 else d[None]
+                for n in range(d3.shape[0]):
+                    de = max(de, abs(0.5 * float(torch.sum(d3[n] * (a[n] - a0[n])))
+                                     - 0.25 * float(torch.sum(d3[n] * (c[n] - c0[n])))))
+            mixed['%g' % split] = {'s_per_batch': t_m, 'speedup_vs_fp64_tuned': t_tuned / t_m,
+                                   'max_abs_diff_vs_fp64': e_max, 'max_abs_dE_2e_Ha': de}
+    except Exception as exc:  # noqa: BLE001
+        mixed = {'error': '%s: %s' % (type(exc).__name__, exc)}
+    finally:
+        b.precision = 'fp64'
     return {'workload': '64 seeded C/N/O/H molecules of 5-40 atoms, syn-6-31g*, 1-4 random PSD densities each',
             'n_molecules': len(mols), 'n_densities': int(sum(d.shape[0] for d in dms)),
             'nao_total': int(sum(m.nao for m, _ in mols)), 'quartets': int(nquart),
             's_per_batch_molecule_loop': t_loop, 's_per_batch_shared_launches': t_eager,
             's_per_batch_tuned': t_tuned, 's_per_batch_graph_replay': t_graph,
             'speedup_graph_vs_loop': t_loop / t_graph, 'autotune_s': t_tune,
-            'quartets_per_s_graph': nquart / t_graph, 'max_abs_diff_vs_loop': err}
+            'quartets_per_s_graph': nquart / t_graph, 'max_abs_diff_vs_loop': err, 'mixed': mixed}
 
 
 def max_over_ranks(seconds, world, device):
