@@ -16,7 +16,7 @@ Works with any molecule object exposing the libcint arrays ``_atm``,
 
 import numpy as np
 
-from .mole import cart2sph_coeff, common_fac_sp, ncart, nsph
+from .mole import cart2sph_coeff, common_fac_sp, ncart
 
 
 class SortedBasis:

@@ -77,7 +77,6 @@ def atom_density(symb, shells, cart=False, max_cycle=60, tol=1e-9):
     J/K and one-electron integrals come from the GPU engine; the tiny
     eigenproblems are solved on the host."""
     import scipy.linalg
-    import torch
     from ..gto.mole import M, charge_of
     from . import hf, jk
     amol = M(atom=[(symb, (0., 0., 0.))], basis={symb: shells}, unit='Bohr', cart=cart)

@@ -30,7 +30,7 @@ import numpy as np
 import torch
 
 from ..gto import M
-from ..gto.mole import charge_of, std_symbol
+from ..gto.mole import std_symbol
 from . import guess, hf, mlp
 
 ELEMS = ['H', 'C', 'N', 'O']

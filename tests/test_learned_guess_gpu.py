@@ -1,7 +1,6 @@
 """Learned initial guess end to end on a small set: converged densities from
 the engine's RHF, training on the network kernels, held-out SCF from the
 predicted density versus the superposition-of-atoms guess."""
-import numpy as np
 import pytest
 
 pytestmark = pytest.mark.gpu

@@ -87,7 +87,6 @@ def test_rsh_mixed_precision():
 
 
 def test_rsh_c_abi_errors():
-    import ctypes
     import torch
     from gpu4pyscf_gb300.lib import libjk
     from gpu4pyscf_gb300.scf import jk
