@@ -80,6 +80,7 @@ struct Shell {
     const double *coef;  // [nctr][nprim]
     double r[3];
     int ao0;             // first Cartesian AO index
+    int atom;
 };
 
 std::vector<Shell> make_shells(const int *atm, const int *bas, int nbas, const double *env, int *nao_out) {
@@ -96,6 +97,7 @@ std::vector<Shell> make_shells(const int *atm, const int *bas, int nbas, const d
         const double *r = env + atm[b[ATOM_OF] * 6 + PTR_COORD];
         s.r[0] = r[0]; s.r[1] = r[1]; s.r[2] = r[2];
         s.ao0 = off;
+        s.atom = b[ATOM_OF];
         off += ncart(s.l) * s.nctr;
     }
     *nao_out = off;
@@ -494,6 +496,101 @@ int oracle_jk(const int *atm, int natm, const int *bas, int nbas, const double *
                 for (size_t x = 0; x < nn * n_dm; ++x) vk[x] += kbuf[t][x];
     }
     if (stats) { stats[0] = n_comp; stats[1] = n_skip; stats[2] = n_prim; stats[3] = npair; }
+    return 0;
+}
+
+// Nuclear gradient of the two-electron energy of one symmetric density D
+// (Cartesian AO basis of the shells) at fixed D,
+//   E = j_factor/2 sum (ij|kl) D_ji D_lk - k_factor/4 sum (ij|kl) D_jk D_li,
+// grad[A*3+x] = dE/dR_Ax.  This is what gpu4pyscf's RYS_per_atom_jk_ip1
+// returns for an RHF density (gpu4pyscf/lib/gvhf-rys/rys_contract_jk_ip1.cu:
+// 1747-1797, called by _jk_energy_per_atom, gpu4pyscf/grad/rhf.py:60-171;
+// its own check is gpu4pyscf/scf/tests/test_scf_jk.py:388-413).
+// With D symmetric the four centres of a quartet contribute alike, so
+//   dE/dR_A = -4 sum_{i on A} sum_jkl (d/dr_i i j|kl) G_ijkl,
+//   G_ijkl = j_factor/2 D_ji D_lk - k_factor/4 D_jk D_li,
+// and the derivative of a Cartesian primitive x^a exp(-alpha r^2) along x is
+// a x^(a-1) exp(..) - 2 alpha x^(a+1) exp(..): the ERIs of the shell raised
+// by one (coefficients times 2 alpha) and lowered by one.  No screening.
+int oracle_jk_grad(const int *atm, int natm, const int *bas, int nbas, const double *env,
+                   const double *dm, double j_factor, double k_factor, double *grad, int nthreads) {
+    int nao;
+    auto sh = make_shells(atm, bas, nbas, env, &nao);
+    const double omega = env[PTR_RANGE_OMEGA];
+    for (int i = 0; i < natm * 3; ++i) grad[i] = 0.;
+    int nt = nthreads_of(nthreads);
+    std::vector<std::vector<double>> gbuf(nt, std::vector<double>((size_t)natm * 3, 0.));
+#pragma omp parallel for schedule(dynamic) num_threads(nt)
+    for (int ish = 0; ish < nbas; ++ish) {
+#ifdef _OPENMP
+        std::vector<double> &g = gbuf[omp_get_thread_num()];
+#else
+        std::vector<double> &g = gbuf[0];
+#endif
+        const Shell &I = sh[ish];
+        // raised (coefficients x 2 alpha) and lowered copies of shell I
+        std::vector<double> cplus((size_t)I.nctr * I.nprim);
+        for (int c = 0; c < I.nctr; ++c)
+            for (int p = 0; p < I.nprim; ++p) cplus[c * I.nprim + p] = I.coef[c * I.nprim + p] * 2. * I.exps[p];
+        Shell Ip = I, Im = I;
+        Ip.l = I.l + 1;
+        Ip.coef = cplus.data();
+        Im.l = I.l - 1;
+        std::vector<int> ax, ay, az, px, py, pz, mx, my, mz;
+        cart_comps(I.l, ax, ay, az);
+        cart_comps(Ip.l, px, py, pz);
+        if (I.l > 0) cart_comps(Im.l, mx, my, mz);
+        auto find = [](const std::vector<int> &X, const std::vector<int> &Y, const std::vector<int> &Z,
+                       int x, int y, int z) {
+            for (size_t c = 0; c < X.size(); ++c)
+                if (X[c] == x && Y[c] == y && Z[c] == z) return (int)c;
+            return -1;
+        };
+        const int nfi = ncart(I.l), nfp = ncart(Ip.l), nfm = I.l > 0 ? ncart(Im.l) : 0;
+        std::vector<double> bp, bm;
+        for (int jsh = 0; jsh < nbas; ++jsh)
+        for (int ksh = 0; ksh < nbas; ++ksh)
+        for (int lsh = 0; lsh < nbas; ++lsh) {
+            const Shell &J = sh[jsh], &K = sh[ksh], &L = sh[lsh];
+            eri_block(Ip, J, K, L, bp, omega);
+            if (I.l > 0) eri_block(Im, J, K, L, bm, omega);
+            const int nfj = ncart(J.l), nfk = ncart(K.l), nfl = ncart(L.l);
+            const int nrest = nfj * nfk * nfl;
+            for (int ci = 0; ci < I.nctr; ++ci)
+            for (int cj = 0; cj < J.nctr; ++cj)
+            for (int ck = 0; ck < K.nctr; ++ck)
+            for (int cl = 0; cl < L.nctr; ++cl) {
+                const size_t cidx = ((ci * J.nctr + cj) * K.nctr + ck) * L.nctr + cl;
+                const double *op = bp.data() + cidx * (size_t)nfp * nrest;
+                const double *om = I.l > 0 ? bm.data() + cidx * (size_t)nfm * nrest : nullptr;
+                for (int a = 0; a < nfi; ++a) {
+                    const size_t Ia = aoidx(I, ci, a);
+                    for (int x = 0; x < 3; ++x) {
+                        const int d[3] = {x == 0, x == 1, x == 2};
+                        const int up = find(px, py, pz, ax[a] + d[0], ay[a] + d[1], az[a] + d[2]);
+                        const int na = x == 0 ? ax[a] : (x == 1 ? ay[a] : az[a]);
+                        const int dn = na > 0 ? find(mx, my, mz, ax[a] - d[0], ay[a] - d[1], az[a] - d[2]) : -1;
+                        double s = 0.;
+                        for (int b = 0; b < nfj; ++b)
+                        for (int c = 0; c < nfk; ++c)
+                        for (int e = 0; e < nfl; ++e) {
+                            const int r = (b * nfk + c) * nfl + e;
+                            // d/dr of the bra function: a_x (a-1) - 2 alpha (a+1)
+                            double deri = -op[(size_t)up * nrest + r];
+                            if (dn >= 0) deri += na * om[(size_t)dn * nrest + r];
+                            const size_t Jb = aoidx(J, cj, b), Kc = aoidx(K, ck, c), Le = aoidx(L, cl, e);
+                            const double G = .5 * j_factor * dm[Jb * nao + Ia] * dm[Le * nao + Kc]
+                                           - .25 * k_factor * dm[Jb * nao + Kc] * dm[Le * nao + Ia];
+                            s += deri * G;
+                        }
+                        g[I.atom * 3 + x] -= 4. * s;
+                    }
+                }
+            }
+        }
+    }
+    for (int t = 0; t < nt; ++t)
+        for (int i = 0; i < natm * 3; ++i) grad[i] += gbuf[t][i];
     return 0;
 }
 

@@ -54,7 +54,7 @@ def lib():
         if _lib is None:
             build()
             _lib = ctypes.CDLL(_LIB_PATH)
-            for name in ('oracle_eri_full', 'oracle_qcond', 'oracle_jk', 'oracle_int1e'):
+            for name in ('oracle_eri_full', 'oracle_qcond', 'oracle_jk', 'oracle_int1e', 'oracle_jk_grad'):
                 getattr(_lib, name).restype = ctypes.c_int
     return _lib
 
@@ -184,6 +184,22 @@ def get_jk_cart(mol, dm_cart, hermi=1, tol=0., with_j=True, with_k=True,
     if err:
         raise RuntimeError('oracle_jk failed')
     return vj.reshape(shape), vk.reshape(shape), stats
+
+
+def jk_energy_grad(mol, dm, j_factor=1., k_factor=1., nthreads=0):
+    """[natm, 3] nuclear gradient of E = j/2 sum (ij|kl) D_ji D_lk
+    - k/4 sum (ij|kl) D_jk D_li at fixed symmetric user-basis density D: what
+    gpu4pyscf's _jk_energy_per_atom returns for an RHF density
+    (gpu4pyscf/grad/rhf.py:60-171)."""
+    atm, bas, env = _env_args(mol)
+    C = ao_c_matrix(mol)
+    dmc = np.ascontiguousarray(C @ np.asarray(dm, dtype=np.float64) @ C.T)
+    g = np.zeros((mol.natm, 3))
+    err = lib().oracle_jk_grad(_p(atm), len(atm), _p(bas), len(bas), _p(env), _p(dmc),
+                               ctypes.c_double(j_factor), ctypes.c_double(k_factor), _p(g), int(nthreads))
+    if err:
+        raise RuntimeError('oracle_jk_grad failed')
+    return g
 
 
 def get_jk(mol, dm, hermi=1, tol=0., with_j=True, with_k=True, nthreads=0):
