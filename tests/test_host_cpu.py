@@ -78,3 +78,33 @@ def test_bad_arguments_rejected_without_gpu():
     assert lib.jk_opt_create(None, 0, None, 0, None, 0, 1e-13, 0, ctypes.byref(h)) == -1
     assert b'invalid' in lib.jk_last_error()
     assert lib.jk_build(None, None, 1, 1, 1, 1, 1, 0, 0., None, None, None, None) == -1
+
+
+def _header_arity(path):
+    """{function name: number of parameters} of the prototypes in a header."""
+    text = open(path).read()
+    text = re.sub(r'/\*.*?\*/', '', text, flags=re.S)
+    out = {}
+    for m in re.finditer(r'^[A-Za-z_][\w \*]*?\b((?:jk|mlp)_\w+)\s*\(([^)]*)\)\s*;', text, re.M):
+        args = m.group(2).strip()
+        out[m.group(1)] = 0 if args in ('', 'void') else len(args.split(','))
+    return out
+
+
+def test_ctypes_signatures_match_headers():
+    """The ctypes bindings (the reference-side stub a maintainer would add)
+    declare exactly the parameters of the C prototypes."""
+    from gpu4pyscf_gb300.lib import libjk
+    from gpu4pyscf_gb300.scf import mlp
+    lib = libjk.load()
+    arity = _header_arity(os.path.join(ROOT, 'include', 'gb300jk.h'))
+    arity.update(_header_arity(os.path.join(ROOT, 'include', 'gb300mlp.h')))
+    mlp._lib()
+    checked = 0
+    for name, n in arity.items():
+        f = getattr(lib, name)
+        if f.argtypes is None:
+            continue
+        assert len(f.argtypes) == n, (name, len(f.argtypes), n)
+        checked += 1
+    assert checked >= 20
