@@ -1,0 +1,48 @@
+"""Nuclear gradient of the J/K energy on the GPU (scf/grad_jk.py: the
+engine's J/K of the extended basis) against the oracle's analytic gradient
+(pinned by finite differences in tests/test_oracle_grad.py).  Follows the
+reference's check of _jk_energy_per_atom against int2e_ip1 contractions
+(gpu4pyscf/scf/tests/test_scf_jk.py:388-413).  Collected after the J/K
+parity tests it builds on (and before the allocation-free test, which must
+come last)."""
+import numpy as np
+import pytest
+
+from gpu4pyscf_gb300 import gto
+from oracle import oracle as orc
+
+pytestmark = pytest.mark.gpu
+
+H2O = 'O 0 0.1 0.2; H -1.4 0.1 -0.8; H 1.5 -0.2 -0.7'
+
+
+@pytest.mark.parametrize('basis, cart, jf, kf, omega', [
+    ('syn-6-31g*', False, 1., .5, 0.),
+    ('syn-cc-pvdz', True, 1., 1., 0.),
+    ('syn-def2-svp', False, 0., 1., 0.),
+    ('syn-6-31g*', False, 0., 1., -0.3),
+])
+def test_grad_vs_oracle(basis, cart, jf, kf, omega):
+    from gpu4pyscf_gb300.scf import grad_jk
+    mol = gto.M(atom=H2O, basis=basis, unit='B', cart=cart)
+    mol.omega = omega
+    rng = np.random.default_rng(6)
+    a = rng.random((mol.nao, mol.nao)) - .5
+    dm = a @ a.T
+    g = grad_jk.jk_energy_grad(mol, dm, jf, kf, direct_scf_tol=1e-15).cpu().numpy()
+    ref = orc.jk_energy_grad(mol, dm, jf, kf)
+    scale = max(1., abs(ref).max())
+    assert abs(g - ref).max() < 1e-9 * scale
+    assert abs(g.sum(axis=0)).max() < 1e-9 * scale
+
+
+def test_reference_entry():
+    from gpu4pyscf_gb300.scf import grad_jk, jk
+    mol = gto.M(atom='O 0 0.7375 -0.0528; O 0 -0.7375 -0.1528', basis='syn-def2-svp')
+    rng = np.random.default_rng(12)
+    a = rng.random((mol.nao, mol.nao)) - .5
+    dm = a @ a.T
+    opt = jk._VHFOpt(mol).build()
+    e = grad_jk._jk_energy_per_atom(opt, dm, j_factor=1., k_factor=.5)
+    ref = orc.jk_energy_grad(mol, dm, 1., .5)
+    assert abs(e - ref).max() < 1e-8 * max(1., abs(ref).max())
