@@ -67,14 +67,19 @@ def make_density(mol):
 
 
 class ClockSampler:
+    """nvidia-smi clock and throttle-reason samples every 200 ms while the
+    timed region runs (read only: no setting of the GPU is touched),
+    summarised as the median SM clock and the reasons seen."""
+
     def __init__(self):
         self.proc = None
-        self.path = os.path.join(ROOT, 'gpurun_out', 'clocks_bench.csv')
+        self.path = None
 
     def start(self):
         try:
-            os.makedirs(os.path.dirname(self.path), exist_ok=True)
-            self.fh = open(self.path, 'w')
+            import tempfile
+            fd, self.path = tempfile.mkstemp(prefix='jk_clocks_', suffix='.csv')
+            self.fh = os.fdopen(fd, 'w')
             self.proc = subprocess.Popen(
                 ['nvidia-smi', '--query-gpu=index,clocks.sm,clocks.max.sm,power.draw,'
                  'clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,'
@@ -104,6 +109,10 @@ class ClockSampler:
             for n, v in zip(names, t[5:9]):
                 if v.lower().startswith('active'):
                     reasons.add(n)
+        try:
+            os.unlink(self.path)
+        except OSError:
+            pass
         if not sm:
             return None
         return {'sm_mhz': float(np.median(sm)), 'sm_max_mhz': smax, 'reasons': sorted(reasons),
