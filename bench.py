@@ -88,6 +88,12 @@ class ClockSampler:
                 stdout=self.fh, stderr=subprocess.DEVNULL)
         except Exception:
             self.proc = None
+            if self.path:
+                try:
+                    self.fh.close()
+                    os.unlink(self.path)
+                except Exception:
+                    pass
 
     def stop(self):
         if self.proc is None:
