@@ -125,8 +125,11 @@ class ClockSampler:
                 'samples': len(sm)}
 
 
-def cpu_sample(mol, dm_user, target_s=15.):
-    """Time the C++ oracle on a bounded sample of the same J/K build."""
+def cpu_sample(mol, dm_user, target_s=15., min_stride=1):
+    """Time the C++ oracle on a bounded sample of the same J/K build: every
+    stride-th bra shell pair, the stride shrunk until the sample takes a
+    quarter of target_s or more (stride 1 is the whole build, whose J/K are
+    returned as 'vj', 'vk' in the sorted Cartesian basis)."""
     from oracle import oracle
     from gpu4pyscf_gb300.gto.sorted_basis import SortedBasis
     sb = SortedBasis(mol)
@@ -136,21 +139,51 @@ def cpu_sample(mol, dm_user, target_s=15.):
     dms = sb.coeff @ dm_user @ sb.coeff.T
     npair = sb.nbas * (sb.nbas + 1) // 2
     cores = os.cpu_count()
-    # every stride-th bra shell pair: shrink the stride until the sample
-    # takes a quarter of the target time or more
-    stride = max(npair // 64, 1)
+    stride = max(npair // 64, min_stride, 1)
     while True:
         t0 = time.perf_counter()
-        _, _, st = oracle.get_jk_cart(Raw, dms, hermi=1, tol=1e-13, nthreads=cores, bra_stride=stride)
+        vj, vk, st = oracle.get_jk_cart(Raw, dms, hermi=1, tol=1e-13, nthreads=cores, bra_stride=stride)
         dt = time.perf_counter() - t0
-        if dt > target_s / 4 or stride == 1:
+        if dt > target_s / 4 or stride <= min_stride:
             break
-        stride = max(1, int(stride / max(2., target_s / 4 / max(dt, 1e-3))))
+        stride = max(min_stride, int(stride / max(2., target_s / 4 / max(dt, 1e-3))))
     return {'value': float(st[0]) / dt, 'unit': 'quartets/s', 'cores': cores, 'kind': 'port',
             'sample': 'C++ McMurchie-Davidson oracle (OpenMP, %d threads), every %d-th of %d bra shell '
                       'pairs of the same sorted basis and density: %d quartets in %.2f s'
                       % (cores, stride, npair, st[0], dt),
-            'seconds': dt, 'quartets': int(st[0]), 'stride': stride}
+            'seconds': dt, 'quartets': int(st[0]), 'stride': stride,
+            'vj': vj if stride == 1 else None, 'vk': vk if stride == 1 else None}
+
+
+def oracle_full(mol, dm_user):
+    """The oracle's whole J/K build of the benchmark density (sorted
+    Cartesian basis, hermi=1, tol 1e-13) on all host cores, timed: the
+    parity reference of the bench line and its CPU baseline."""
+    from oracle import oracle
+    from gpu4pyscf_gb300.gto.sorted_basis import SortedBasis
+    sb = SortedBasis(mol)
+
+    class Raw:
+        _atm, _bas, _env = sb._atm, sb._bas, sb._env
+    dms = sb.coeff @ dm_user @ sb.coeff.T
+    cores = os.cpu_count()
+    t0 = time.perf_counter()
+    vj, vk, st = oracle.get_jk_cart(Raw, dms, hermi=1, tol=1e-13, nthreads=cores)
+    dt = time.perf_counter() - t0
+    base = {'value': float(st[0]) / dt, 'unit': 'quartets/s', 'cores': cores, 'kind': 'port',
+            'sample': 'C++ McMurchie-Davidson oracle (OpenMP, %d threads), the whole build: every bra '
+                      'shell pair of the same sorted basis and density, %d quartets in %.2f s'
+                      % (cores, st[0], dt)}
+    return dms, vj, vk, base
+
+
+def parity_vs_oracle(vj, vk, ref_j, ref_k, dm_sorted):
+    """Max |dJ|, |dK| and the two-electron energy difference of a build
+    against the oracle's J/K of the same sorted density (FP64 bar: 1e-10)."""
+    dj = vj - ref_j
+    dk = vk - ref_k
+    de = 0.5 * float(np.sum(dm_sorted * dj)) - 0.25 * float(np.sum(dm_sorted * dk))
+    return {'max_abs_dJ': float(abs(dj).max()), 'max_abs_dK': float(abs(dk).max()), 'dE_2e_Ha': de}
 
 
 def run_reference(args):
@@ -158,10 +191,11 @@ def run_reference(args):
     if rank != 0:
         return
     mol = make_mol(args.config)
-    dm = make_density_cpu(mol)
-    ts, qs = [], 0
+    dm, dm_source = reference_density(mol)
+    ts = []
     for _ in range(args.warmup):
-        pass
+        # a short sample of the same build (thread pool, caches, pages)
+        cpu_sample(mol, dm, target_s=min(4., args.ref_seconds), min_stride=8)
     res = None
     for _ in range(args.steps):
         res = cpu_sample(mol, dm, target_s=args.ref_seconds)
@@ -171,16 +205,25 @@ def run_reference(args):
             'n_gpus': args.gpus, 'steps': args.steps, 'warmup': args.warmup,
             'ms_per_step': 1e3 * float(np.mean(ts)), 'higher_is_better': True, 'scaling': 'weak',
             'vs_baseline': None, 'dtype': 'f64', 'data': 'synthetic',
-            'config': {'workload': CONFIGS[args.config]['workload'], 'nao_user': mol.nao},
+            'config': {'workload': CONFIGS[args.config]['workload'], 'nao_user': mol.nao,
+                       'density': dm_source},
             'cpu_baseline': {k: res[k] for k in ('value', 'unit', 'cores', 'kind', 'sample')},
             'e2e': {'value': val, 'unit': 'quartets/s', 'h2d_bytes_per_step': 0, 'd2h_bytes_per_step': 0}}
     print(json.dumps(line))
 
 
-def make_density_cpu(mol):
-    """SAD density from the oracle's atomic SCF (CPU only)."""
+def reference_density(mol):
+    """The density of the GPU arm (the engine's SAD guess) when a GPU is
+    present, so both arms build J/K of the same matrix; otherwise the
+    oracle's SAD, the same guess restated on the CPU."""
+    try:
+        import torch
+        if torch.cuda.is_available():
+            return make_density(mol), 'SAD (engine, as the GPU arm)'
+    except Exception:  # noqa: BLE001
+        pass
     from oracle import oracle
-    return oracle.sad_density(mol)
+    return oracle.sad_density(mol), 'SAD (oracle restatement; no GPU)'
 
 
 def fma_peak(lib, fp32):
@@ -392,6 +435,17 @@ def run_scf(args):
     print(json.dumps(line))
 
 
+def dense_density(mol):
+    """The density after the first SCF step from SAD (dense: what every later
+    Fock build of an SCF sees), with the RHF object that made it."""
+    from gpu4pyscf_gb300.scf import hf
+    mf = hf.RHF(mol)
+    dm0 = mf.get_init_guess()
+    f = mf.get_hcore() + mf.get_veff(None, dm0)
+    e, c = mf.eig(f)
+    return mf.make_rdm1(c, mf.get_occ(e, c)), mf
+
+
 def dense_mixed(mol, splits=(1e-6, 1e-4)):
     """J/K of a dense SCF density of mol (the density after the first SCF
     step from SAD, what every later Fock build of an SCF sees), FP64 against
@@ -401,12 +455,8 @@ def dense_mixed(mol, splits=(1e-6, 1e-4)):
     atom, which the density screening exploits; this is the build of the SCF
     iterations."""
     import torch
-    from gpu4pyscf_gb300.scf import hf, jk
-    mf = hf.RHF(mol)
-    dm0 = mf.get_init_guess()
-    f = mf.get_hcore() + mf.get_veff(None, dm0)
-    e, c = mf.eig(f)
-    dm = mf.make_rdm1(c, mf.get_occ(e, c))
+    from gpu4pyscf_gb300.scf import jk
+    dm, mf = dense_density(mol)
     opt = mf.opt
     rows = []
     ref = None
@@ -504,6 +554,8 @@ def run_gpu(args):
     dmc = dms[0]
     t64s = sum(t64) / args.steps
 
+    mixed_results = {}
+
     def mixed_eval(split, prec, steps):
         opt.precision, opt.split_thresh = prec, split
         nvtx_push('jk_mixed_%g_%s' % (split, prec))
@@ -515,6 +567,7 @@ def run_gpu(args):
             fn()
         tm = sum(timed(fn, steps)) / steps
         vjm, vkm = opt._build(dms, 1, True, True)
+        mixed_results['mixed_%g_%s' % (split, prec)] = (vjm, vkm)
         de = float((0.5 * torch.sum(dmc * (vjm[0] - vj64[0]))
                     - 0.25 * torch.sum(dmc * (vkm[0] - vk64[0]))).item())
         opt.precision = 'fp64'
@@ -531,6 +584,8 @@ def run_gpu(args):
     for split in (1e-8, 1e-6, 1e-4, 1e-3, 1e-2):
         for prec in ('mixed', 'mixed-fp32roots'):
             r = mixed_eval(split, prec, 2)
+            if split not in (1e-8, 1e-6):
+                mixed_results.pop('mixed_%g_%s' % (split, prec), None)
             sweep.append([split, prec, round(r['s_per_jk_build'], 5), round(r['speedup_vs_fp64'], 3),
                           r['max_abs_dJ_sorted'], r['max_abs_dK_sorted'], r['dE_2e_Ha']])
     mixed['sweep'] = {'columns': ['split', 'precision', 's_per_jk_build', 'speedup_vs_fp64',
@@ -591,6 +646,8 @@ def run_gpu(args):
     traffic = NCU_DRAM_BYTES.get((args.config, dom['class']))
     roofline = {'bound': 'fp64', 'achieved': achieved, 'peak': peak64 / 1e12, 'unit': 'TFLOP/s',
                 'frac': achieved / (peak64 / 1e12), 'traffic': traffic,
+                'traffic_source': ('DRAM read + write of one launch of this class from the committed ncu '
+                                   'capture (profiles/), not measured in this run' if traffic else None),
                 'kernel': '%s %s FP64' % (kernel_family(*lk4), dom['class']), 'dominant': dom,
                 'peak_source': 'FP64 FMA-chain probe measured in this run (MEASURED_PEAKS.json has no FP64 figure)',
                 'fp32_peak_tflops': peak32 / 1e12,
@@ -633,10 +690,22 @@ def run_gpu(args):
     except Exception as exc:  # noqa: BLE001
         mixed_dense = {'error': '%s: %s' % (type(exc).__name__, exc)}
 
-    cpu = None
+    # the oracle's whole build of the same density: parity of the FP64 and
+    # mixed builds, and the CPU baseline (rank 0, N=1); configurations whose
+    # whole oracle build would take minutes fall back to a strided sample
+    # and report no parity
+    cpu, parity = None, None
     if rank == 0 and world == 1 and not args.no_cpu:
-        cpu = cpu_sample(mol, dm, target_s=args.cpu_seconds)
-        cpu = {k: cpu[k] for k in ('value', 'unit', 'cores', 'kind', 'sample')}
+        if args.config in ('c30', 'c10', 'h2o'):
+            dm_s, ref_j, ref_k, cpu = oracle_full(mol, dm)
+            parity = {'vs': 'oracle (C++ McMurchie-Davidson, tol 1e-13), same sorted density',
+                      'tolerance_fp64': 1e-10, 'tolerance_mixed_elementwise': 1e-7,
+                      'fp64': parity_vs_oracle(vj64[0].cpu().numpy(), vk64[0].cpu().numpy(), ref_j, ref_k, dm_s)}
+            for key, (vjm, vkm) in mixed_results.items():
+                parity[key] = parity_vs_oracle(vjm[0].cpu().numpy(), vkm[0].cpu().numpy(), ref_j, ref_k, dm_s)
+        else:
+            cpu = cpu_sample(mol, dm, target_s=args.cpu_seconds)
+            cpu = {k: cpu[k] for k in ('value', 'unit', 'cores', 'kind', 'sample')}
 
     if rank == 0:
         line = {'metric': 'jk_quartets_per_s', 'value': value, 'unit': 'quartets/s', 'n_gpus': world,
@@ -653,7 +722,7 @@ def run_gpu(args):
                         'd2h_bytes_per_step': 2 * nbytes, 's_per_step': sum(te) / args.steps},
                 'gpu_launches': int(st64['kernel_launches']) * args.steps,
                 'mixed': mixed, 'mixed_dense': mixed_dense, 'roofline': roofline, 'classes_top': per_class[:8],
-                'batched': batched, 'cpu_baseline': cpu, 'clocks': clock_info}
+                'batched': batched, 'cpu_baseline': cpu, 'parity': parity, 'clocks': clock_info}
         print(json.dumps(line))
     if world > 1:
         dist.destroy_process_group()

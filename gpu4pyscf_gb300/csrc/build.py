@@ -22,13 +22,19 @@ FLAGS = ['-O3', '-std=c++17', '-lineinfo', '-Xcompiler', '-fPIC', '-diag-suppres
          '-I' + HERE, '-I' + os.path.join(ROOT, 'include')]
 NBRA = 10
 
-SOURCES = ['jk_device.cuh', 'jk_kernel.cuh', 'rys_roots.cuh', 'rys_tables.inc', 'jk_registry.h',
-           'jk_classes.cu', 'jk_engine.cu', 'int1e.cu', 'mlp.cu', 'build.py']
+# every file of this directory that can reach the library: a change to any
+# of them forces a rebuild
+SOURCE_EXTS = ('.cu', '.cuh', '.h', '.inc', '.py')
+
+
+def _sources():
+    return sorted(f for f in os.listdir(HERE) if f.endswith(SOURCE_EXTS))
 
 
 def _digest():
     h = hashlib.sha256()
-    for f in SOURCES:
+    for f in _sources():
+        h.update(f.encode())
         with open(os.path.join(HERE, f), 'rb') as fh:
             h.update(fh.read())
     for hdr in ('gb300jk.h', 'gb300mlp.h'):

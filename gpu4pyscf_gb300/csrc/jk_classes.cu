@@ -28,7 +28,7 @@ static void reg_one(ClassEntry *tab) {
     if constexpr (COST <= LEAN_MAX) {
         e.lean64 = 1;
         e.k64 = (const void *)rys_lean_kernel<LI, LJ, LK, LL, double>;
-        e.qb64 = LEAN_THREADS; e.smem64 = 0; e.threads64 = LEAN_THREADS;
+        e.qb64 = LEAN_THREADS; e.smem64 = LeanSmem<LI, LJ, LK, LL, double>::BYTES; e.threads64 = LEAN_THREADS;
         e.k64_alt = (const void *)rys_class_kernel<LI, LJ, LK, LL, double, MODE_JK>;
         e.smem64_alt = S64::SMEM;
     } else {
@@ -40,7 +40,7 @@ static void reg_one(ClassEntry *tab) {
     if constexpr (COST <= LEAN_MAX_F32) {
         e.lean32 = 1;
         e.k32 = (const void *)rys_lean_kernel<LI, LJ, LK, LL, float>;
-        e.qb32 = LEAN_THREADS; e.smem32 = 0; e.threads32 = LEAN_THREADS;
+        e.qb32 = LEAN_THREADS; e.smem32 = LeanSmem<LI, LJ, LK, LL, float>::BYTES; e.threads32 = LEAN_THREADS;
         e.k32_alt = (const void *)rys_class_kernel<LI, LJ, LK, LL, float, MODE_JK>;
         e.smem32_alt = S32::SMEM;
     } else {

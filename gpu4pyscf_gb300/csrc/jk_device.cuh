@@ -75,6 +75,7 @@ struct EngineDev {
     const int *mol_ndm;       // densities each molecule carries (null: all n_dm)
     int with_j, with_k;
     float log_cut;
+    float log_split;          // mixed builds: log of the FP64/FP32 split threshold
     int fp32_asym;            // 1: FP32 quartets take the large-T asymptote in FP32 too
     // range separation: omega2 = omega^2 > 0 evaluates erf(omega r)/r instead
     // of 1/r (rys_roots_rs); op_scale multiplies every integral (a negative
@@ -99,11 +100,19 @@ struct ClassDev {
     const int *ket_begin;     // [nx]
     const int *ket_end;       // [nx]
     int *work;                // range counter of this launch (zeroed per build)
+    // which screened quartets of the ranges this launch computes:
+    // SPLIT_ALL every one, SPLIT_HIGH those whose bound reaches the split
+    // (FP64 part of a mixed build), SPLIT_LOW those below it (FP32 part)
+    int split_mode;
 };
+
+enum { SPLIT_ALL = 0, SPLIT_HIGH = 1, SPLIT_LOW = 2 };
 
 // Screening of (bra, ket) of a class: q_ij q_kl times the largest of the six
 // density blocks the quartet touches against the cutoff
-// (gpu4pyscf/lib/gvhf-rys/create_tasks.cu:152-162).
+// (gpu4pyscf/lib/gvhf-rys/create_tasks.cu:152-162).  In a mixed build the
+// same bound, the quartet's own, decides its precision: FP64 when it reaches
+// the split threshold, FP32 below it.
 __device__ __forceinline__ bool pair_passes(const EngineDev &d, const ClassDev &c, int bra, int ket) {
     const int2 pij = c.bra.ij[bra], pkl = c.ket.ij[ket];
     const float *dc = d.dm_cond;
@@ -111,53 +120,43 @@ __device__ __forceinline__ bool pair_passes(const EngineDev &d, const ClassDev &
     float dmax = fmaxf(fmaxf(__ldg(dc + pij.x * nb + pij.y), __ldg(dc + pkl.x * nb + pkl.y)),
                        fmaxf(fmaxf(__ldg(dc + pij.x * nb + pkl.x), __ldg(dc + pij.x * nb + pkl.y)),
                              fmaxf(__ldg(dc + pij.y * nb + pkl.x), __ldg(dc + pij.y * nb + pkl.y))));
-    return __ldg(c.bra.logq + bra) + __ldg(c.ket.logq + ket) + dmax >= d.log_cut;
+    const float v = __ldg(c.bra.logq + bra) + __ldg(c.ket.logq + ket) + dmax;
+    if (!(v >= d.log_cut)) return false;
+    if (c.split_mode == SPLIT_HIGH) return v >= d.log_split;
+    if (c.split_mode == SPLIT_LOW) return v < d.log_split;
+    return true;
 }
 
 // kets per work unit: a range [ket_begin[x], ket_end[x]) is cut into units
 // of JK_KCHUNK kets, numbered through the class by q_off (unit prefix sums)
 #define JK_KCHUNK 64
 
-// work unit w -> range x and its ket interval [k0, k1)
-__device__ __forceinline__ void unit_at(const ClassDev &c, int w, int &x, int &k0, int &k1) {
-    int lo = 0, hi = c.nx;
+// work unit w -> range x and its ket interval [k0, k1), found by the 32
+// lanes of a warp together (all must call it with the same w): each step
+// probes 32 evenly spaced unit offsets with one load per lane and keeps the
+// interval between the last offset <= w and the next, so a search over nx
+// ranges takes log32(nx) dependent loads instead of log2(nx).
+__device__ __forceinline__ void unit_at_warp(const ClassDev &c, int w, int lane, int &x, int &k0, int &k1) {
+    int lo = 0, hi = c.nx;   // q_off[lo] <= w < q_off[hi]
     while (hi - lo > 1) {
-        int mid = (lo + hi) >> 1;
-        if (__ldg(c.q_off + mid) <= w) lo = mid; else hi = mid;
+        const int step = (hi - lo + 31) >> 5;
+        const int p = lo + lane * step;
+        const bool le = p < hi && __ldg(c.q_off + p) <= w;
+        const unsigned m = __ballot_sync(0xffffffffu, le);
+        const int t = 31 - __clz(m);   // lane 0 probes lo, so m != 0
+        lo += t * step;
+        hi = min(hi, lo + step);
     }
     x = lo;
     k0 = __ldg(c.ket_begin + lo) + (w - __ldg(c.q_off + lo)) * JK_KCHUNK;
     k1 = min(__ldg(c.ket_end + lo), k0 + JK_KCHUNK);
 }
 
-__device__ __forceinline__ void quartet_at(const ClassDev &c, int g, int &x, int &bra, int &ket);
-
-// Density screening of quartet g of the class numbering: q_ij q_kl times the
-// largest of the six density blocks it touches against the cutoff
-// (gpu4pyscf/lib/gvhf-rys/create_tasks.cu:152-162).
-__device__ __forceinline__ bool quartet_passes(const EngineDev &d, const ClassDev &c, int g) {
-    int x, bra, ket;
-    quartet_at(c, g, x, bra, ket);
-    const int2 pij = c.bra.ij[bra], pkl = c.ket.ij[ket];
-    const float *dc = d.dm_cond;
-    const int nb = d.nbas;
-    float dmax = fmaxf(fmaxf(__ldg(dc + pij.x * nb + pij.y), __ldg(dc + pkl.x * nb + pkl.y)),
-                       fmaxf(fmaxf(__ldg(dc + pij.x * nb + pkl.x), __ldg(dc + pij.x * nb + pkl.y)),
-                             fmaxf(__ldg(dc + pij.y * nb + pkl.x), __ldg(dc + pij.y * nb + pkl.y))));
-    return __ldg(c.bra.logq + bra) + __ldg(c.ket.logq + ket) + dmax >= d.log_cut;
-}
-
-// quartet g -> (range x, bra, ket)
-__device__ __forceinline__ void quartet_at(const ClassDev &c, int g, int &x, int &bra, int &ket) {
-    int lo = 0, hi = c.nx;
-    while (hi - lo > 1) {
-        int mid = (lo + hi) >> 1;
-        if (__ldg(c.q_off + mid) <= g) lo = mid; else hi = mid;
-    }
-    x = lo;
-    bra = lo % c.bra.n;
-    ket = __ldg(c.ket_begin + lo) + (g - __ldg(c.q_off + lo));
-}
+// A launch's warps (lean family) or blocks (cooperative family) beyond one
+// per JK_MIN_UNITS work units return at once: in classes with little work
+// the remaining ones then run full warps instead of many warps with a few
+// quartets each.
+#define JK_MIN_UNITS 8
 
 __host__ __device__ constexpr int ncart(int l) { return (l + 1) * (l + 2) / 2; }
 

@@ -185,11 +185,16 @@ __device__ int count_ge(const float *q, int n, float thr) {
     return lo;
 }
 
-// Per (ket bucket, bra pair): the ket range passing q_ij q_kl max|D| >= tol
-// and, in mixed mode, its split into an FP64 head and an FP32 tail; the
-// counts are the work units of each range, scanned into unit offsets.
+// Per (ket bucket, bra pair): the ket range that can pass
+// q_ij q_kl max|D| >= tol with the largest density block, and in mixed mode
+// the two overlapping ranges the FP64 and FP32 launches scan: kets before
+// beg32 reach the split even with the bra's own density block (FP64 for
+// sure), kets from mid on stay below it even with the largest block (FP32
+// for sure); in between the kernels decide per quartet from its own six
+// blocks.  The counts are the work units of each range, scanned into unit
+// offsets.
 __global__ void plan_kernel(const PlanClass *pcs, int npc, int total, const float *dm_max,
-                            float log_cut, float log_split, int mixed) {
+                            const float *dm_cond, int nbas, float log_cut, float log_split, int mixed) {
     int g = blockIdx.x * blockDim.x + threadIdx.x;
     if (g >= total) return;
     int lo = 0, hi = npc;
@@ -212,18 +217,24 @@ __global__ void plan_kernel(const PlanClass *pcs, int npc, int total, const floa
     int b0 = p.ket_bstart[k], b1 = p.ket_bstart[k + 1];
     float base = p.bra_logq[ib] + dm_max[0];
     int end = b0 + count_ge(p.ket_logq + b0, b1 - b0, log_cut - base);
-    int mid = end;
-    if (mixed) mid = min(end, b0 + count_ge(p.ket_logq + b0, b1 - b0, log_split - base));
+    int mid = end, beg32 = end;
+    if (mixed) {
+        mid = min(end, b0 + count_ge(p.ket_logq + b0, b1 - b0, log_split - base));
+        const int2 ij = p.bra_ij[ib];
+        const float own = p.bra_logq[ib] + dm_cond[(size_t)ij.x * nbas + ij.y];
+        beg32 = min(end, b0 + count_ge(p.ket_logq + b0, b1 - b0, log_split - own));
+    }
     if (p.same) {
         end = max(b0, min(end, ib + 1));
         mid = max(b0, min(mid, ib + 1));
+        beg32 = max(b0, min(beg32, ib + 1));
     }
     p.kb64[x] = b0;
     p.ke64[x] = mid;
     p.cnt64[x] = (mid - b0 + JK_KCHUNK - 1) / JK_KCHUNK;
-    p.kb32[x] = mid;
+    p.kb32[x] = beg32;
     p.ke32[x] = end;
-    p.cnt32[x] = mixed ? (end - mid + JK_KCHUNK - 1) / JK_KCHUNK : 0;
+    p.cnt32[x] = mixed ? (end - beg32 + JK_KCHUNK - 1) / JK_KCHUNK : 0;
 }
 
 struct ScanJob { const int *cnt; int *off; int n; };
@@ -466,8 +477,8 @@ int launch_class(const void *func, int grid, int smem, const EngineDev &d, const
 int set_smem_attrs() {
     for (int q = 0; q < NQCLASS; ++q) {
         const ClassEntry &e = g_tab[q];
-        if (e.k64 && !e.lean64) CK(cudaFuncSetAttribute(e.k64, cudaFuncAttributeMaxDynamicSharedMemorySize, e.smem64));
-        if (e.k32 && !e.lean32) CK(cudaFuncSetAttribute(e.k32, cudaFuncAttributeMaxDynamicSharedMemorySize, e.smem32));
+        if (e.k64) CK(cudaFuncSetAttribute(e.k64, cudaFuncAttributeMaxDynamicSharedMemorySize, e.smem64));
+        if (e.k32) CK(cudaFuncSetAttribute(e.k32, cudaFuncAttributeMaxDynamicSharedMemorySize, e.smem32));
         if (e.kdiag) CK(cudaFuncSetAttribute(e.kdiag, cudaFuncAttributeMaxDynamicSharedMemorySize, e.smemdiag));
         if (e.k64_alt) CK(cudaFuncSetAttribute(e.k64_alt, cudaFuncAttributeMaxDynamicSharedMemorySize, e.smem64_alt));
         if (e.k32_alt) CK(cudaFuncSetAttribute(e.k32_alt, cudaFuncAttributeMaxDynamicSharedMemorySize, e.smem32_alt));
@@ -739,12 +750,9 @@ static int create_impl(const int32_t *atm, int natm, const int32_t *bas, int nba
         for (int pc = 0; pc < NPAIRCLASS; ++pc) { cudaFree(dij[pc]); cudaFree(dpo[pc]); cudaFree(dpc[pc]); cudaFree(dq[pc]); }
         cudaFree(ca); cudaFree(cb); cudaFree(cip);
         if (err) return bail(err);
-        // prune and sort
-        double qmax = 0.;
-        for (int pc = 0; pc < NPAIRCLASS; ++pc)
-            for (float v : qh[pc]) qmax = std::max(qmax, (double)v);
-        // keep a pair if it can reach tol with density blocks up to 1e4
-        double keep = tol > 0 ? tol / (std::max(qmax, 1e-300) * 1e4) : 0.;
+        // sort; every pair with a nonzero Schwarz factor is kept whatever
+        // the densities of later builds (the per-build plan cuts the ket
+        // ranges by the actual density maxima)
         o->qcond_h.assign((size_t)nbas * nbas, 0.);
         PrimPairHost fpp;
         for (int pc = 0; pc < NPAIRCLASS; ++pc) {
@@ -752,7 +760,7 @@ static int create_impl(const int32_t *atm, int natm, const int32_t *bas, int nba
             for (int k = 0; k < (int)qh[pc].size(); ++k) {
                 const int2 &p = cand[pc].ij[k];
                 o->qcond_h[(size_t)p.x * nbas + p.y] = o->qcond_h[(size_t)p.y * nbas + p.x] = qh[pc][k];
-                if (qh[pc][k] > 0 && qh[pc][k] >= keep) idx.push_back(k);
+                if (qh[pc][k] > 0) idx.push_back(k);
             }
             std::vector<int> pruned(qh[pc].size(), 0);
             for (int k : idx) pruned[k] = count_prim_pairs(o, cand[pc].ij[k].x, cand[pc].ij[k].y);
@@ -948,7 +956,7 @@ static int build_impl(jk_opt *o, const double *dm, int n_dm, int hermi, int with
         float log_cut = o->tol > 0 ? (float)std::log(o->tol) : -1e30f;
         float log_split = mixed ? (float)std::log(split_thresh) : 0.f;
         plan_kernel<<<(o->plan_total + 255) / 256, 256, 0, st>>>(o->plan_dev, o->nplan, o->plan_total, o->dm_max,
-                                                                 log_cut, log_split, mixed);
+                                                                 o->dm_cond, o->nbas, log_cut, log_split, mixed);
         scan_kernel<<<o->nscan, 1024, 0, st>>>(o->scan_dev);
         launches += 2;
     }
@@ -967,6 +975,7 @@ static int build_impl(jk_opt *o, const double *dm, int n_dm, int hermi, int with
     d.with_j = with_j && hermi != 2;
     d.with_k = with_k;
     d.log_cut = o->tol > 0 ? (float)std::log(o->tol) : -1e30f;
+    d.log_split = mixed ? (float)std::log(split_thresh) : 0.f;
     d.fp32_asym = precision == JK_PREC_MIXED_FP32ROOTS;
     o->ev_slot.clear();
     if (o->time_classes) {
@@ -1010,6 +1019,7 @@ static int build_impl(jk_opt *o, const double *dm, int n_dm, int hermi, int with
             d.counters = want_stats ? o->counters : nullptr;
             c.work = work + 2 * q;
             c.q_off = o->off64[q]; c.ket_begin = o->kb64[q]; c.ket_end = o->ke64[q];
+            c.split_mode = mixed ? SPLIT_HIGH : SPLIT_ALL;
             if (o->time_classes) { o->ev_slot.push_back(2 * q); CK(cudaEventRecord(o->ev[2 * (o->ev_slot.size() - 1)], st)); }
             if (int er = launch_variant(o, q, 0, upper, d, c, ls)) return er;
             if (o->time_classes) CK(cudaEventRecord(o->ev[2 * (o->ev_slot.size() - 1) + 1], st));
@@ -1018,6 +1028,7 @@ static int build_impl(jk_opt *o, const double *dm, int n_dm, int hermi, int with
                 c.class_id = NQCLASS + q;  // FP32 counters in the second half
                 c.work = work + 2 * q + 1;
                 c.q_off = o->off32[q]; c.ket_begin = o->kb32[q]; c.ket_end = o->ke32[q];
+                c.split_mode = SPLIT_LOW;
                 long long up32 = (long long)o->npairs[a] * ((o->npairs[b] + e.qb32 - 1) / e.qb32 + o->nbk[b]);
                 if (o->time_classes) { o->ev_slot.push_back(2 * q + 1); CK(cudaEventRecord(o->ev[2 * (o->ev_slot.size() - 1)], st)); }
                 cudaStream_t ls32 = concurrent ? o->side[nlaunched++ % jk_opt::NSIDE] : st;
@@ -1141,6 +1152,7 @@ int jk_opt_tune(jk_opt *o, const double *dm, int n_dm, int hermi, int precision,
     d.with_j = hermi != 2;
     d.with_k = 1;
     d.log_cut = o->tol > 0 ? (float)std::log(o->tol) : -1e30f;
+    d.log_split = mixed ? (float)std::log(split_thresh) : 0.f;
     d.fp32_asym = precision == JK_PREC_MIXED_FP32ROOTS;
     static const int grids[4] = {1, 2, 4, 8};
     for (size_t t = 0; !err && t < o->plan_classes.size(); ++t) {
@@ -1163,6 +1175,7 @@ int jk_opt_tune(jk_opt *o, const double *dm, int n_dm, int hermi, int precision,
             c.q_off = prec ? o->off32[q] : o->off64[q];
             c.ket_begin = prec ? o->kb32[q] : o->kb64[q];
             c.ket_end = prec ? o->ke32[q] : o->ke64[q];
+            c.split_mode = !mixed ? SPLIT_ALL : prec ? SPLIT_LOW : SPLIT_HIGH;
             float best = 1e30f;
             int best_alt = 0, best_grid = 0;
             for (int alt = 0; alt <= ((prec ? e.k32_alt : e.k64_alt) ? 1 : 0) && !err; ++alt)
@@ -1199,11 +1212,10 @@ int jk_opt_tune(jk_opt *o, const double *dm, int n_dm, int hermi, int precision,
 // ---------------------------------------------------------------------------
 // Allocation-free J/K build.
 //
-// Some callers cannot call cudaMalloc at the moment they need a J/K build:
-// code that runs while a CUDA stream is being captured into a graph (a
-// capture is invalidated by an allocation), a host running under a strict
-// device-memory budget that forbids growth after start-up, or a plugin
-// sandbox whose host framework owns every allocation.  jk_build grows its
+// Some callers cannot call cudaMalloc at the moment they need a J/K build: a
+// process running under a strict device-memory budget that forbids growth
+// after start-up, or a plugin inside a host application whose own framework
+// owns every device allocation.  jk_build grows its
 // per-call workspace on demand; jk_build_noalloc instead takes every
 // per-call buffer (density copies, J/K accumulators, screening table) from
 // the fixed device array below, which each GPU that loads this library holds
@@ -1251,11 +1263,11 @@ extern "C" int jk_build_noalloc(jk_opt *o, const double *dm, int n_dm, int nao, 
     if (!o || !dm || n_dm <= 0 || o->nmol != 1 || nao != o->nao || hermi < 0 || hermi > 2 || (!with_j && !with_k))
         return fail(JK_ERR_ARG, "jk_build_noalloc: invalid arguments");
     if ((with_j && !vj) || (with_k && !vk)) return fail(JK_ERR_ARG, "jk_build_noalloc: missing output buffer");
-    if (precision != JK_PREC_FP64 && precision != JK_PREC_MIXED)
+    if (precision != JK_PREC_FP64 && precision != JK_PREC_MIXED && precision != JK_PREC_MIXED_FP32ROOTS)
         return fail(JK_ERR_ARG, "jk_build_noalloc: bad precision");
-    if (precision == JK_PREC_MIXED && !(split_thresh > 0))
+    if (precision != JK_PREC_FP64 && !(split_thresh > 0))
         return fail(JK_ERR_ARG, "jk_build_noalloc: split_thresh must be > 0");
-    const int mixed = precision == JK_PREC_MIXED;
+    const int mixed = precision != JK_PREC_FP64;
     const size_t nn = (size_t)nao * nao;
     const int n_dmk = hermi == 0 ? 2 * n_dm : n_dm;
     // carve the scratch: dmj, dmk, jt, kt, [dmj_f, dmk_f], dm_cond, dm_max
@@ -1297,7 +1309,7 @@ extern "C" int jk_build_noalloc(jk_opt *o, const double *dm, int n_dm, int nao, 
         float log_cut = o->tol > 0 ? (float)std::log(o->tol) : -1e30f;
         float log_split = mixed ? (float)std::log(split_thresh) : 0.f;
         plan_kernel<<<(o->plan_total + 255) / 256, 256, 0, st>>>(o->plan_dev, o->nplan, o->plan_total, dm_max,
-                                                                 log_cut, log_split, mixed);
+                                                                 dm_cond, o->nbas, log_cut, log_split, mixed);
         scan_kernel<<<o->nscan, 1024, 0, st>>>(o->scan_dev);
     }
     CK(cudaGetLastError());
@@ -1313,8 +1325,12 @@ extern "C" int jk_build_noalloc(jk_opt *o, const double *dm, int n_dm, int nao, 
     d.with_j = with_j && hermi != 2;
     d.with_k = with_k;
     d.log_cut = o->tol > 0 ? (float)std::log(o->tol) : -1e30f;
+    d.log_split = mixed ? (float)std::log(split_thresh) : 0.f;
+    d.fp32_asym = precision == JK_PREC_MIXED_FP32ROOTS;
     d.counters = nullptr;
     if (d.with_j || d.with_k) {
+        // the optimizer's launch variants (autotuned or set), one class after
+        // another on the caller's stream
         for (int q : o->plan_classes) {
             const ClassEntry &e = g_tab[q];
             int a = 0;
@@ -1330,14 +1346,16 @@ extern "C" int jk_build_noalloc(jk_opt *o, const double *dm, int n_dm, int nao, 
             c.class_id = q;
             c.work = work + 2 * q;
             c.q_off = o->off64[q]; c.ket_begin = o->kb64[q]; c.ket_end = o->ke64[q];
+            c.split_mode = mixed ? SPLIT_HIGH : SPLIT_ALL;
             long long upper = (long long)o->npairs[a] * ((o->npairs[bcls] + e.qb64 - 1) / e.qb64 + o->nbk[bcls]);
-            if (int er = launch_class(e.k64, grid_for(o, upper, e.lean64), e.smem64, d, c, 0, st, e.threads64)) return er;
+            if (int er = launch_variant(o, q, 0, upper, d, c, st)) return er;
             if (mixed) {
                 c.class_id = NQCLASS + q;
                 c.work = work + 2 * q + 1;
                 c.q_off = o->off32[q]; c.ket_begin = o->kb32[q]; c.ket_end = o->ke32[q];
+                c.split_mode = SPLIT_LOW;
                 long long up32 = (long long)o->npairs[a] * ((o->npairs[bcls] + e.qb32 - 1) / e.qb32 + o->nbk[bcls]);
-                if (int er = launch_class(e.k32, grid_for(o, up32, e.lean32), e.smem32, d, c, 0, st, e.threads32)) return er;
+                if (int er = launch_variant(o, q, 1, up32, d, c, st)) return er;
             }
         }
     }

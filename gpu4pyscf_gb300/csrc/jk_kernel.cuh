@@ -39,8 +39,11 @@ __device__ __forceinline__ const float *dm_ptr<float>(const EngineDev &d, bool j
     return jpart ? d.dmj_f + idm * nn : d.dmk_f + idm * nn;
 }
 
+// Two blocks per SM (at most 128 registers a thread): while one block's few
+// root-evaluating threads run stage S1, the other block keeps the FP64
+// pipes busy with its S2/S3 work.
 template <int LI, int LJ, int LK, int LL, typename Real, int MODE>
-__global__ void __launch_bounds__(JK_THREADS)
+__global__ void __launch_bounds__(JK_THREADS, 2)
 rys_class_kernel(EngineDev d, ClassDev c, int ntiles_static)
 {
     using S = ClassShape<LI, LJ, LK, LL, Real>;
@@ -93,9 +96,10 @@ rys_class_kernel(EngineDev d, ClassDev c, int ntiles_static)
     // full.  Schwarz mode: fixed tiles of pairs.
     __shared__ int2 bq[MODE == MODE_JK ? QB + JK_THREADS : 1];
     __shared__ int wcnt[JK_THREADS / 32];
-    __shared__ int s_base;
+    __shared__ int s_unit[4];
     int chunk = blockIdx.x;
     const int nunits = MODE == MODE_JK ? __ldg(c.q_off + c.nx) : 0;
+    if (MODE == MODE_JK && blockIdx.x > 0 && (long long)blockIdx.x * JK_MIN_UNITS >= nunits) return;
     int kcur = 0, kend = 0, bcur = 0;
     bool exhausted = false;
     int nq = 0;
@@ -104,14 +108,27 @@ rys_class_kernel(EngineDev d, ClassDev c, int ntiles_static)
         if (MODE == MODE_JK) {
             while (nq < QB && !exhausted) {
                 if (kcur >= kend) {
-                    if (tid == 0) s_base = atomicAdd(c.work, 1);
+                    // warp 0 takes the next unit and finds its range
+                    if (tid < 32) {
+                        int w = 0;
+                        if (tid == 0) w = atomicAdd(c.work, 1);
+                        w = __shfl_sync(0xffffffffu, w, 0);
+                        int xw = 0, k0 = 0, k1 = 0;
+                        if (w < nunits) unit_at_warp(c, w, tid, xw, k0, k1);
+                        if (tid == 0) {
+                            s_unit[0] = w;
+                            s_unit[1] = xw % c.bra.n;
+                            s_unit[2] = k0;
+                            s_unit[3] = k1;
+                        }
+                    }
                     __syncthreads();
-                    const int w = s_base;
+                    const int w = s_unit[0];
+                    bcur = s_unit[1];
+                    kcur = s_unit[2];
+                    kend = s_unit[3];
                     __syncthreads();
                     if (w >= nunits) { exhausted = true; break; }
-                    int xw;
-                    unit_at(c, w, xw, kcur, kend);
-                    bcur = xw % c.bra.n;
                     continue;
                 }
                 const int kk = kcur + tid;

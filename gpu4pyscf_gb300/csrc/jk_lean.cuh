@@ -1,16 +1,17 @@
 // Register-resident Rys J/K kernel for the small angular classes.
 //
-// One thread owns one shell quartet from start to end, with no block
-// barriers.  Each warp takes (ket bucket, bra) ranges from a work counter,
-// screens their kets and queues the survivors, so its 32 lanes run 32
-// quartets with the same ket primitive count at a time.  Per primitive quartet and root the
-// 2D integrals of the three axes live in registers (fully unrolled vertical
-// recurrence and horizontal transfers), the Cartesian ERI block accumulates
-// in registers, and after the primitive loops the thread contracts its block
-// with the six density blocks.  The J block of the bra pair, common to the
-// warp when all its lanes share the bra pair, is summed across the warp with
-// shuffles before one atomic add per element; the four K blocks go out with
-// one atomic add per distinct address of the warp, J_kl directly.
+// One thread owns one shell quartet at a time, with no block barriers.  Per
+// primitive quartet and root the 2D integrals of the three axes live in
+// registers (fully unrolled vertical recurrence and horizontal transfers)
+// and the Cartesian ERI block accumulates in registers.  Quartets differ in
+// their primitive-pair counts, so lanes are refilled one by one: each warp
+// iteration runs one primitive quartet on every busy lane, a lane whose
+// quartet is complete stages its ERI block in shared memory and takes the
+// next quartet from the warp's queue of screened (bra, ket) pairs, and the
+// warp digests staged blocks 32 at a time (every lane one quartet: the six
+// contractions with the density blocks, added to J and K with one atomic
+// per element).  The FP64 pipe, GB300's scarcest, so sees full warps except
+// at the very end of a launch.
 #pragma once
 #include "jk_device.cuh"
 #include "rys_roots.cuh"
@@ -124,20 +125,186 @@ template <> struct LeanIO<float> {
     static __device__ __forceinline__ const float *dk(const EngineDev &d) { return d.dmk_f; }
 };
 
+// Finished quartets of a warp wait in shared memory until 32 of them can be
+// digested together: their ERI blocks as [NF][LEAN_STAGE] (quartet index
+// fastest, so the lanes of a warp hit consecutive banks) and their
+// (bra, ket) indices.  LEAN_STAGE = 64 holds the at most 31 waiting plus 32
+// newly finished quartets of one step.
+#define LEAN_STAGE 64
+
+template <int LI, int LJ, int LK, int LL, typename Real>
+struct LeanSmem {
+    static constexpr int NF = LeanShape<LI, LJ, LK, LL>::NF;
+    static constexpr int WARPS = LEAN_THREADS / 32;
+    static constexpr int BYTES = WARPS * LEAN_STAGE * (NF * (int)sizeof(Real) + (int)sizeof(int2));
+};
+
+// Adds v to *addr for every lane with a non-null addr.  FP64 quartets add
+// lane by lane: the atomics resolve in L2 and cost the FP64 pipe nothing,
+// where summing lanes first would.  FP32 quartets sum lanes that hit the same
+// element in FP32 (warp aggregation) and convert once.  All 32 lanes call it.
+template <typename Real>
+__device__ __forceinline__ void lean_add(double *addr, Real v, Real *buf, int lane) {
+    if constexpr (sizeof(Real) == 8) {
+        if (addr != nullptr) atomicAdd(addr, v);
+    } else {
+        warp_agg_add(addr, v, buf, lane);
+    }
+}
+
+// Digestion of n staged quartets (lane l takes slot l < n; n >= 1): the six
+// contractions of each quartet's ERI block with the density blocks it
+// touches, added to J and K.
+template <int LI, int LJ, int LK, int LL, typename Real>
+__device__ __forceinline__ void lean_digest(const EngineDev &d, const ClassDev &c, const Real *st, const int2 *sq,
+                                            int n, Real *aggbuf, int lane) {
+    using S = LeanShape<LI, LJ, LK, LL>;
+    constexpr int NFI = S::NFI, NFJ = S::NFJ, NFK = S::NFK, NFL = S::NFL;
+    const bool valid = lane < n;
+    const int2 q = sq[valid ? lane : 0];
+    const int2 pij = c.bra.ij[q.x], pkl = c.ket.ij[q.y];
+    const ShellDev &A = d.shells[pij.x];
+    const int mol = A.mol;
+    const int nao = __ldg(d.mol_nao + mol);
+    const size_t nn = (size_t)d.ntot;
+    const size_t mbase = (size_t)__ldg(d.mol_base + mol);
+    const int ndm_m = d.mol_ndm ? __ldg(d.mol_ndm + mol) : d.n_dm;
+    const Real fac = Real((pij.x == pij.y ? .5 : 1.) * (pkl.x == pkl.y ? .5 : 1.) *
+                          (c.same && q.x == q.y ? .5 : 1.));
+    const int ai = A.ao, aj = d.shells[pij.y].ao;
+    const int ak = d.shells[pkl.x].ao, al = d.shells[pkl.y].ao;
+    const Real *E = st + lane;   // element e of this lane's quartet: E[e * LEAN_STAGE]
+#define LEAN_E(a, b, cc, dd) E[((((a) * NFJ + (b)) * NFK + (cc)) * NFL + (dd)) * LEAN_STAGE]
+    if (d.with_j) {
+        for (int idm = 0; idm < d.n_dm; ++idm) {
+            // densities the molecule does not carry are skipped
+            const bool vd = valid && idm < ndm_m;
+            if (!__any_sync(0xffffffffu, vd)) continue;
+            const Real *Dm = LeanIO<Real>::dj(d) + idm * nn + mbase;
+            double *V = d.vj + idm * nn + mbase;
+            Real dkl[NFK * NFL], dij[NFI * NFJ];
+#pragma unroll
+            for (int cc = 0; cc < NFK; ++cc)
+#pragma unroll
+                for (int dd = 0; dd < NFL; ++dd) dkl[cc * NFL + dd] = Dm[(size_t)(ak + cc) * nao + al + dd];
+#pragma unroll
+            for (int a = 0; a < NFI; ++a)
+#pragma unroll
+                for (int b = 0; b < NFJ; ++b) dij[a * NFJ + b] = Dm[(size_t)(ai + a) * nao + aj + b];
+#pragma unroll
+            for (int a = 0; a < NFI; ++a)
+#pragma unroll
+                for (int b = 0; b < NFJ; ++b) {   // J[ij] += E D[kl]
+                    Real s = Real(0);
+#pragma unroll
+                    for (int cc = 0; cc < NFK; ++cc)
+#pragma unroll
+                        for (int dd = 0; dd < NFL; ++dd) s += LEAN_E(a, b, cc, dd) * dkl[cc * NFL + dd];
+                    lean_add(vd ? V + (size_t)(ai + a) * nao + aj + b : nullptr, fac * s, aggbuf, lane);
+                }
+#pragma unroll
+            for (int cc = 0; cc < NFK; ++cc)
+#pragma unroll
+                for (int dd = 0; dd < NFL; ++dd) {   // J[kl] += E D[ij]
+                    Real s = Real(0);
+#pragma unroll
+                    for (int a = 0; a < NFI; ++a)
+#pragma unroll
+                        for (int b = 0; b < NFJ; ++b) s += LEAN_E(a, b, cc, dd) * dij[a * NFJ + b];
+                    lean_add(vd ? V + (size_t)(ak + cc) * nao + al + dd : nullptr, fac * s, aggbuf, lane);
+                }
+        }
+    }
+    if (d.with_k) {
+        for (int idm = 0; idm < d.n_dmk; ++idm) {
+            const bool vd = valid && (idm % d.n_dm) < ndm_m;
+            if (!__any_sync(0xffffffffu, vd)) continue;
+            const Real *Dm = LeanIO<Real>::dk(d) + idm * nn + mbase;
+            double *V = d.vk + idm * nn + mbase;
+            Real djl[NFJ * NFL], djk[NFJ * NFK], dil[NFI * NFL], dik[NFI * NFK];
+#pragma unroll
+            for (int b = 0; b < NFJ; ++b) {
+#pragma unroll
+                for (int dd = 0; dd < NFL; ++dd) djl[b * NFL + dd] = Dm[(size_t)(aj + b) * nao + al + dd];
+#pragma unroll
+                for (int cc = 0; cc < NFK; ++cc) djk[b * NFK + cc] = Dm[(size_t)(aj + b) * nao + ak + cc];
+            }
+#pragma unroll
+            for (int a = 0; a < NFI; ++a) {
+#pragma unroll
+                for (int dd = 0; dd < NFL; ++dd) dil[a * NFL + dd] = Dm[(size_t)(ai + a) * nao + al + dd];
+#pragma unroll
+                for (int cc = 0; cc < NFK; ++cc) dik[a * NFK + cc] = Dm[(size_t)(ai + a) * nao + ak + cc];
+            }
+#pragma unroll
+            for (int a = 0; a < NFI; ++a)
+#pragma unroll
+                for (int cc = 0; cc < NFK; ++cc) {   // K[i a, k c] += E D[j b, l d]
+                    Real s = Real(0);
+#pragma unroll
+                    for (int b = 0; b < NFJ; ++b)
+#pragma unroll
+                        for (int dd = 0; dd < NFL; ++dd) s += LEAN_E(a, b, cc, dd) * djl[b * NFL + dd];
+                    lean_add(vd ? V + (size_t)(ai + a) * nao + ak + cc : nullptr, fac * s, aggbuf, lane);
+                }
+#pragma unroll
+            for (int a = 0; a < NFI; ++a)
+#pragma unroll
+                for (int dd = 0; dd < NFL; ++dd) {   // K[i a, l d] += E D[j b, k c]
+                    Real s = Real(0);
+#pragma unroll
+                    for (int b = 0; b < NFJ; ++b)
+#pragma unroll
+                        for (int cc = 0; cc < NFK; ++cc) s += LEAN_E(a, b, cc, dd) * djk[b * NFK + cc];
+                    lean_add(vd ? V + (size_t)(ai + a) * nao + al + dd : nullptr, fac * s, aggbuf, lane);
+                }
+#pragma unroll
+            for (int b = 0; b < NFJ; ++b)
+#pragma unroll
+                for (int cc = 0; cc < NFK; ++cc) {   // K[j b, k c] += E D[i a, l d]
+                    Real s = Real(0);
+#pragma unroll
+                    for (int a = 0; a < NFI; ++a)
+#pragma unroll
+                        for (int dd = 0; dd < NFL; ++dd) s += LEAN_E(a, b, cc, dd) * dil[a * NFL + dd];
+                    lean_add(vd ? V + (size_t)(aj + b) * nao + ak + cc : nullptr, fac * s, aggbuf, lane);
+                }
+#pragma unroll
+            for (int b = 0; b < NFJ; ++b)
+#pragma unroll
+                for (int dd = 0; dd < NFL; ++dd) {   // K[j b, l d] += E D[i a, k c]
+                    Real s = Real(0);
+#pragma unroll
+                    for (int a = 0; a < NFI; ++a)
+#pragma unroll
+                        for (int cc = 0; cc < NFK; ++cc) s += LEAN_E(a, b, cc, dd) * dik[a * NFK + cc];
+                    lean_add(vd ? V + (size_t)(aj + b) * nao + al + dd : nullptr, fac * s, aggbuf, lane);
+                }
+        }
+    }
+#undef LEAN_E
+}
+
 template <int LI, int LJ, int LK, int LL, typename Real>
 __global__ void __launch_bounds__(LEAN_THREADS)
 rys_lean_kernel(EngineDev d, ClassDev c, int unused)
 {
     using S = LeanShape<LI, LJ, LK, LL>;
-    constexpr int NR = S::NR, NF = S::NF, GS = S::GS, GSKL = S::GSKL;
+    constexpr int NR = S::NR, NF = S::NF, GS = S::GS;
     constexpr int NFI = S::NFI, NFJ = S::NFJ, NFK = S::NFK, NFL = S::NFL;
-    const int lane = threadIdx.x & 31;
-    // Per-warp work: the warp takes work units (JK_KCHUNK kets of one
-    // (bucket, bra) range) from the launch's counter, screens their kets 32 at
-    // a time and queues the quartets that pass; each iteration runs 32 queued
-    // quartets.
-    __shared__ int2 queue[LEAN_THREADS / 32][64];
-    __shared__ Real aggbuf[LEAN_THREADS / 32][32];
+    constexpr unsigned FULL = 0xffffffffu;
+    constexpr int WARPS = LEAN_THREADS / 32;
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    const unsigned lt = (1u << lane) - 1u;
+    // Per warp: a queue of screened quartets (bra, ket) waiting for a lane,
+    // the staging area of finished ERI blocks, and the buffer of the FP32
+    // warp aggregation.
+    __shared__ int2 queue[WARPS][64];
+    __shared__ Real aggbuf[WARPS][32];
+    extern __shared__ __align__(16) unsigned char lean_smem[];
+    Real *stage = reinterpret_cast<Real *>(lean_smem) + (size_t)wid * NF * LEAN_STAGE;
+    int2 *stage_q = reinterpret_cast<int2 *>(reinterpret_cast<Real *>(lean_smem) + (size_t)WARPS * NF * LEAN_STAGE) +
+                    wid * LEAN_STAGE;
     // FP32: the Rys table block of this class in shared memory (the lanes'
     // T values fall in different intervals; global loads of the table would
     // cost one L1 wavefront per interval, shared loads one per instruction)
@@ -147,269 +314,188 @@ rys_lean_kernel(EngineDev d, ClassDev c, int unused)
         rys_stage_f<NR>(d.rys_coef_f, s_rys, threadIdx.x, blockDim.x);
         __syncthreads();
     }
-    int2 *wq = queue[threadIdx.x >> 5];
-    Real *ab_buf = aggbuf[threadIdx.x >> 5];
+    int2 *wq = queue[wid];
+    Real *ab_buf = aggbuf[wid];
     const int nunits = __ldg(c.q_off + c.nx);
+    const int gwarp = (blockIdx.x * LEAN_THREADS + threadIdx.x) >> 5;
+    if (gwarp > 0 && (long long)gwarp * JK_MIN_UNITS >= nunits) return;
     int kcur = 0, kend = 0, bcur = 0;
     bool exhausted = false;
-    int nq = 0;
+    int nq = 0, nst = 0;
+    // the lane's quartet: indices, primitive-pair offsets and counters,
+    // centre differences and the ERI block accumulated so far
+    bool has = false;
+    int qb = 0, qk = 0, pb0 = 0, pk0 = 0, npk = 1, pbi = 0, pki = 0, left = 0;
+    Real abx = 0, aby = 0, abz = 0, cdx = 0, cdy = 0, cdz = 0;
+    Real acc[NF];
+#pragma unroll
+    for (int e = 0; e < NF; ++e) acc[e] = Real(0);
     while (true) {
-        while (nq < 32 && !exhausted) {
-            if (kcur >= kend) {
-                int w = 0;
-                if (lane == 0) w = atomicAdd(c.work, 1);
-                w = __shfl_sync(0xffffffffu, w, 0);
-                if (w >= nunits) { exhausted = true; break; }
-                int xw;
-                unit_at(c, w, xw, kcur, kend);
-                bcur = xw % c.bra.n;
-                continue;
+        // ---- lanes without a quartet take the next ones from the queue,
+        // which is refilled from work units (JK_KCHUNK kets of one
+        // (bucket, bra) range, screened 32 at a time) as needed
+        const unsigned empty = __ballot_sync(FULL, !has);
+        if (empty) {
+            const int need = __popc(empty);
+            while (nq < need && !exhausted) {
+                if (kcur >= kend) {
+                    int w = 0;
+                    if (lane == 0) w = atomicAdd(c.work, 1);
+                    w = __shfl_sync(FULL, w, 0);
+                    if (w >= nunits) { exhausted = true; break; }
+                    int xw;
+                    unit_at_warp(c, w, lane, xw, kcur, kend);
+                    bcur = xw % c.bra.n;
+                    continue;
+                }
+                const int kk = kcur + lane;
+                const bool ok = kk < kend && pair_passes(d, c, bcur, kk);
+                const unsigned m = __ballot_sync(FULL, ok);
+                if (ok) wq[nq + __popc(m & lt)] = make_int2(bcur, kk);
+                nq += __popc(m);
+                kcur += 32;
+                __syncwarp();
             }
-            const int kk = kcur + lane;
-            const bool ok = kk < kend && pair_passes(d, c, bcur, kk);
-            const unsigned m = __ballot_sync(0xffffffffu, ok);
-            if (ok) wq[nq + __popc(m & ((1u << lane) - 1u))] = make_int2(bcur, kk);
-            nq += __popc(m);
-            kcur += 32;
-            __syncwarp();
-        }
-        if (nq == 0) break;
-        const int take = min(nq, 32);
-        const int2 mine = lane < take ? wq[lane] : make_int2(-1, -1);
-        __syncwarp();
-        if (nq > 32) {
-            int2 t = lane < nq - 32 ? wq[32 + lane] : make_int2(0, 0);
-            __syncwarp();
-            if (lane < nq - 32) wq[lane] = t;
-        }
-        nq -= take;
-        __syncwarp();
-        const bool valid = mine.x >= 0;
-        // lane 0 always holds a quartet; idle lanes borrow its indices
-        const int lead_b = __shfl_sync(0xffffffffu, mine.x, 0);
-        const int lead_k = __shfl_sync(0xffffffffu, mine.y, 0);
-        const int ib = valid ? mine.x : lead_b;
-        const int ket = valid ? mine.y : lead_k;
-        const int2 pij = c.bra.ij[ib];
-        int2 pkl = make_int2(0, 0);
-        if (valid) pkl = c.ket.ij[ket];
-        // the J block of the bra pair can be summed across the warp when all
-        // its lanes share the bra
-        const bool same_bra = __all_sync(0xffffffffu, ib == __shfl_sync(0xffffffffu, ib, 0));
-        Real acc[NF];
+            const int take = min(nq, need);
+            const int rank = __popc(empty & lt);
+            if (!has && rank < take) {
+                const int2 e = wq[rank];
+                qb = e.x;
+                qk = e.y;
+                const int2 pij = c.bra.ij[qb], pkl = c.ket.ij[qk];
+                const ShellDev &A = d.shells[pij.x], &B = d.shells[pij.y];
+                const ShellDev &C = d.shells[pkl.x], &D = d.shells[pkl.y];
+                abx = Real(A.x - B.x); aby = Real(A.y - B.y); abz = Real(A.z - B.z);
+                cdx = Real(C.x - D.x); cdy = Real(C.y - D.y); cdz = Real(C.z - D.z);
+                pb0 = c.bra.prim_off[qb];
+                pk0 = c.ket.prim_off[qk];
+                const int npb = __ldg(c.bra.prim_cnt + qb);
+                npk = __ldg(c.ket.prim_cnt + qk);
+                left = npb * npk;
+                pbi = 0;
+                pki = 0;
 #pragma unroll
-        for (int e = 0; e < NF; ++e) acc[e] = Real(0);
-        const ShellDev &A = d.shells[pij.x], &B = d.shells[pij.y];
-        const int npb = __ldg(c.bra.prim_cnt + ib);
-        const int pb0 = c.bra.prim_off[ib];
-        int npk = 0, pk0 = 0;
-        Real abx = Real(A.x - B.x), aby = Real(A.y - B.y), abz = Real(A.z - B.z);
-        Real cdx = 0, cdy = 0, cdz = 0;
-        if (valid) {
-            const ShellDev &C = d.shells[pkl.x], &D = d.shells[pkl.y];
-            npk = __ldg(c.ket.prim_cnt + ket);
-            pk0 = c.ket.prim_off[ket];
-            cdx = Real(C.x - D.x); cdy = Real(C.y - D.y); cdz = Real(C.z - D.z);
-            if (d.counters) {
-                atomicAdd(d.counters + 2 * c.class_id, 1ull);
-                atomicAdd(d.counters + 2 * c.class_id + 1, (unsigned long long)(npb * npk));
+                for (int k = 0; k < NF; ++k) acc[k] = Real(0);
+                has = true;
+                if (d.counters) {
+                    atomicAdd(d.counters + 2 * c.class_id, 1ull);
+                    atomicAdd(d.counters + 2 * c.class_id + 1, (unsigned long long)left);
+                }
             }
+            __syncwarp();
+            if (nq > take) {   // drop the taken entries (at most 63 remain)
+                const int rem = nq - take;
+                const int2 t0 = lane < rem ? wq[take + lane] : make_int2(0, 0);
+                const int2 t1 = lane + 32 < rem ? wq[take + 32 + lane] : make_int2(0, 0);
+                __syncwarp();
+                if (lane < rem) wq[lane] = t0;
+                if (lane + 32 < rem) wq[lane + 32] = t1;
+            }
+            nq -= take;
+            __syncwarp();
         }
-        for (int pb = 0; pb < npb; ++pb) {
+        // an empty queue after the refill means the launch's units are
+        // exhausted; the warp ends when its lanes have finished too
+        if (!__any_sync(FULL, has)) break;
+
+        // ---- one primitive quartet of every busy lane
+        if (has) {
+            const int pb = pb0 + pbi, pk = pk0 + pki;
             Real p, Px, Py, Pz, PAx, PAy, PAz, Kb, ipb;
+            Real q, Qx, Qy, Qz, QCx, QCy, QCz, Kk, ipk;
             if constexpr (sizeof(Real) == 8) {
-                d4 a = d.pp_a[pb0 + pb], b = d.pp_b[pb0 + pb];
+                const d4 a = d.pp_a[pb], b = d.pp_b[pb];
                 p = a.x; Px = a.y; Py = a.z; Pz = a.w; PAx = b.x; PAy = b.y; PAz = b.z; Kb = b.w;
-                ipb = d.pp_ip[pb0 + pb];
+                ipb = d.pp_ip[pb];
+                const d4 a2 = d.pp_a[pk], b2 = d.pp_b[pk];
+                q = a2.x; Qx = a2.y; Qy = a2.z; Qz = a2.w; QCx = b2.x; QCy = b2.y; QCz = b2.z; Kk = b2.w;
+                ipk = d.pp_ip[pk];
             } else {
-                float4 a = d.pp_af[pb0 + pb], b = d.pp_bf[pb0 + pb];
+                const float4 a = d.pp_af[pb], b = d.pp_bf[pb];
                 p = a.x; Px = a.y; Py = a.z; Pz = a.w; PAx = b.x; PAy = b.y; PAz = b.z; Kb = b.w;
-                ipb = d.pp_ipf[pb0 + pb];
+                ipb = d.pp_ipf[pb];
+                const float4 a2 = d.pp_af[pk], b2 = d.pp_bf[pk];
+                q = a2.x; Qx = a2.y; Qy = a2.z; Qz = a2.w; QCx = b2.x; QCy = b2.y; QCz = b2.z; Kk = b2.w;
+                ipk = d.pp_ipf[pk];
             }
-            for (int pk = 0; pk < npk; ++pk) {
-                Real q, Qx, Qy, Qz, QCx, QCy, QCz, Kk, ipk;
-                if constexpr (sizeof(Real) == 8) {
-                    d4 a = d.pp_a[pk0 + pk], b = d.pp_b[pk0 + pk];
-                    q = a.x; Qx = a.y; Qy = a.z; Qz = a.w; QCx = b.x; QCy = b.y; QCz = b.z; Kk = b.w;
-                    ipk = d.pp_ip[pk0 + pk];
-                } else {
-                    float4 a = d.pp_af[pk0 + pk], b = d.pp_bf[pk0 + pk];
-                    q = a.x; Qx = a.y; Qy = a.z; Qz = a.w; QCx = b.x; QCy = b.y; QCz = b.z; Kk = b.w;
-                    ipk = d.pp_ipf[pk0 + pk];
-                }
-                Real rs, u[NR], w[NR];
-                const Real PQx = Px - Qx, PQy = Py - Qy, PQz = Pz - Qz;
-                if constexpr (sizeof(Real) == 8) {
-                    rs = rsqrt(p + q);
-                    const double rho = p * q * rs * rs;
-                    double T = rho * (PQx * PQx + PQy * PQy + PQz * PQz);
-                    rys_roots_rs<NR>(T, rho, d.omega2, d.rys_coef, u, w);
-                } else {
-                    rs = rsqrtf(p + q);
-                    const float rho = p * q * rs * rs;
-                    float T = rho * (PQx * PQx + PQy * PQy + PQz * PQz);
-                    rys_roots_rs_f<NR, true>(T, rho, d.omega2_f, s_rys, u, w, d.fp32_asym);
-                }
-                const Real ipq = rs * rs;
-                const Real pref = Real(34.98683665524972497) * Kb * Kk * ipb * ipk * rs *
-                                  (sizeof(Real) == 8 ? Real(d.op_scale) : Real(d.op_scale_f));
-                const Real qpq = q * ipq, ppq = p * ipq;
-                const Real h2p = Real(0.5) * ipb, h2q = Real(0.5) * ipk, h2pq = Real(0.5) * ipq;
-#pragma unroll
-                for (int r = 0; r < NR; ++r) {
-                    const Real ur = u[r];
-                    const Real b00 = ur * h2pq;
-                    const Real b10 = h2p - ur * h2p * qpq;
-                    const Real b01 = h2q - ur * h2q * ppq;
-                    const Real uq = qpq * ur, up = ppq * ur;
-                    Real gx[GS], gy[GS], gz[GS];
-                    rys2d<LI, LJ, LK, LL, Real>(Real(1), PAx - uq * PQx, QCx + up * PQx, b00, b10, b01, abx, cdx, gx);
-                    rys2d<LI, LJ, LK, LL, Real>(Real(1), PAy - uq * PQy, QCy + up * PQy, b00, b10, b01, aby, cdy, gy);
-                    rys2d<LI, LJ, LK, LL, Real>(w[r] * pref, PAz - uq * PQz, QCz + up * PQz, b00, b10, b01, abz, cdz, gz);
-#pragma unroll
-                    for (int a = 0; a < NFI; ++a)
-#pragma unroll
-                        for (int b = 0; b < NFJ; ++b)
-#pragma unroll
-                            for (int cc = 0; cc < NFK; ++cc)
-#pragma unroll
-                                for (int dd = 0; dd < NFL; ++dd) {
-                                    constexpr int dummy = 0;
-                                    (void)dummy;
-                                    const int ix = ((cx_of(LI, a) * (LJ + 1) + cx_of(LJ, b)) * (LK + 1) + cx_of(LK, cc)) * (LL + 1) + cx_of(LL, dd);
-                                    const int iy = ((cy_of(LI, a) * (LJ + 1) + cy_of(LJ, b)) * (LK + 1) + cy_of(LK, cc)) * (LL + 1) + cy_of(LL, dd);
-                                    const int iz = ((cz_of(LI, a) * (LJ + 1) + cz_of(LJ, b)) * (LK + 1) + cz_of(LK, cc)) * (LL + 1) + cz_of(LL, dd);
-                                    acc[((a * NFJ + b) * NFK + cc) * NFL + dd] += gx[ix] * gy[iy] * gz[iz];
-                                }
-                }
+            Real rs, u[NR], w[NR];
+            const Real PQx = Px - Qx, PQy = Py - Qy, PQz = Pz - Qz;
+            if constexpr (sizeof(Real) == 8) {
+                rs = rsqrt(p + q);
+                const double rho = p * q * rs * rs;
+                const double T = rho * (PQx * PQx + PQy * PQy + PQz * PQz);
+                rys_roots_rs<NR>(T, rho, d.omega2, d.rys_coef, u, w);
+            } else {
+                rs = rsqrtf(p + q);
+                const float rho = p * q * rs * rs;
+                const float T = rho * (PQx * PQx + PQy * PQy + PQz * PQz);
+                rys_roots_rs_f<NR, true>(T, rho, d.omega2_f, s_rys, u, w, d.fp32_asym);
             }
+            const Real ipq = rs * rs;
+            const Real pref = Real(34.98683665524972497) * Kb * Kk * ipb * ipk * rs *
+                              (sizeof(Real) == 8 ? Real(d.op_scale) : Real(d.op_scale_f));
+            const Real qpq = q * ipq, ppq = p * ipq;
+            const Real h2p = Real(0.5) * ipb, h2q = Real(0.5) * ipk, h2pq = Real(0.5) * ipq;
+#pragma unroll
+            for (int r = 0; r < NR; ++r) {
+                const Real ur = u[r];
+                const Real b00 = ur * h2pq;
+                const Real b10 = h2p - ur * h2p * qpq;
+                const Real b01 = h2q - ur * h2q * ppq;
+                const Real uq = qpq * ur, up = ppq * ur;
+                Real gx[GS], gy[GS], gz[GS];
+                rys2d<LI, LJ, LK, LL, Real>(Real(1), PAx - uq * PQx, QCx + up * PQx, b00, b10, b01, abx, cdx, gx);
+                rys2d<LI, LJ, LK, LL, Real>(Real(1), PAy - uq * PQy, QCy + up * PQy, b00, b10, b01, aby, cdy, gy);
+                rys2d<LI, LJ, LK, LL, Real>(w[r] * pref, PAz - uq * PQz, QCz + up * PQz, b00, b10, b01, abz, cdz, gz);
+#pragma unroll
+                for (int a = 0; a < NFI; ++a)
+#pragma unroll
+                    for (int b = 0; b < NFJ; ++b)
+#pragma unroll
+                        for (int cc = 0; cc < NFK; ++cc)
+#pragma unroll
+                            for (int dd = 0; dd < NFL; ++dd) {
+                                const int ix = ((cx_of(LI, a) * (LJ + 1) + cx_of(LJ, b)) * (LK + 1) + cx_of(LK, cc)) * (LL + 1) + cx_of(LL, dd);
+                                const int iy = ((cy_of(LI, a) * (LJ + 1) + cy_of(LJ, b)) * (LK + 1) + cy_of(LK, cc)) * (LL + 1) + cy_of(LL, dd);
+                                const int iz = ((cz_of(LI, a) * (LJ + 1) + cz_of(LJ, b)) * (LK + 1) + cz_of(LK, cc)) * (LL + 1) + cz_of(LL, dd);
+                                acc[((a * NFJ + b) * NFK + cc) * NFL + dd] += gx[ix] * gy[iy] * gz[iz];
+                            }
+            }
+            if (++pki == npk) {
+                pki = 0;
+                ++pbi;
+            }
+            --left;
         }
-        // ---- digestion ----
-        const int mol = A.mol;
-        const int nao = __ldg(d.mol_nao + mol);
-        const size_t nn = (size_t)d.ntot;
-        const size_t mbase = (size_t)__ldg(d.mol_base + mol);
-        const int ndm_m = d.mol_ndm ? __ldg(d.mol_ndm + mol) : d.n_dm;
-        const Real fac = Real((pij.x == pij.y ? .5 : 1.) * (pkl.x == pkl.y ? .5 : 1.) *
-                              (c.same && ib == ket ? .5 : 1.));
-        const int ai = A.ao, aj = B.ao;
-        const int ak = valid ? d.shells[pkl.x].ao : 0, al = valid ? d.shells[pkl.y].ao : 0;
-        if (d.with_j) {
-            for (int idm = 0; idm < d.n_dm; ++idm) {
-                // densities the molecule does not carry are skipped
-                const bool vd = valid && idm < ndm_m;
-                if (!__any_sync(0xffffffffu, vd)) continue;
-                const Real *Dm = LeanIO<Real>::dj(d) + idm * nn + mbase;
-                double *V = d.vj + idm * nn + mbase;
-                Real dkl[NFK * NFL], dij[NFI * NFJ];
+
+        // ---- finished quartets: stage their ERI blocks; digest 32 at a time
+        const bool done = has && left == 0;
+        const unsigned fin = __ballot_sync(FULL, done);
+        if (fin) {
+            if (done) {
+                const int slot = nst + __popc(fin & lt);
 #pragma unroll
-                for (int cc = 0; cc < NFK; ++cc)
-#pragma unroll
-                    for (int dd = 0; dd < NFL; ++dd)
-                        dkl[cc * NFL + dd] = vd ? Dm[(size_t)(ak + cc) * nao + al + dd] : Real(0);
-#pragma unroll
-                for (int a = 0; a < NFI; ++a)
-#pragma unroll
-                    for (int b = 0; b < NFJ; ++b) dij[a * NFJ + b] = Dm[(size_t)(ai + a) * nao + aj + b];
-                // J[ij] += sum_kl E D[kl]: same bra for the warp -> shuffle reduction
-#pragma unroll
-                for (int ab = 0; ab < NFI * NFJ; ++ab) {
-                    Real s = Real(0);
-#pragma unroll
-                    for (int cd = 0; cd < NFK * NFL; ++cd) s += acc[ab * NFK * NFL + cd] * dkl[cd];
-                    // (summed across the warp in the kernel's precision,
-                    // converted once for the FP64 accumulator)
-                    Real sd = vd ? fac * s : Real(0);
-                    double *dst = V + (size_t)(ai + ab / NFJ) * nao + aj + ab % NFJ;
-                    if (same_bra) {
-#pragma unroll
-                        for (int off = 16; off > 0; off >>= 1) sd += __shfl_xor_sync(0xffffffffu, sd, off);
-                        if (lane == 0 && sd != Real(0)) atomicAdd(dst, (double)sd);
-                    } else if (vd) {
-                        atomicAdd(dst, (double)sd);
-                    }
-                }
-                if (vd) {
-#pragma unroll
-                    for (int cd = 0; cd < NFK * NFL; ++cd) {
-                        Real s = Real(0);
-#pragma unroll
-                        for (int ab = 0; ab < NFI * NFJ; ++ab) s += acc[ab * NFK * NFL + cd] * dij[ab];
-                        atomicAdd(V + (size_t)(ak + cd / NFL) * nao + al + cd % NFL, (double)(fac * s));
-                    }
-                }
+                for (int e = 0; e < NF; ++e) stage[e * LEAN_STAGE + slot] = acc[e];
+                stage_q[slot] = make_int2(qb, qk);
+                has = false;
             }
-        }
-        if (d.with_k) {
-            // lanes whose kets share a shell hit the same K elements: add
-            // through warp aggregation (idle lanes contribute nothing)
-            for (int idm = 0; idm < d.n_dmk; ++idm) {
-                const bool vd = valid && (idm % d.n_dm) < ndm_m;
-                if (!__any_sync(0xffffffffu, vd)) continue;
-                const Real *Dm = LeanIO<Real>::dk(d) + idm * nn + mbase;
-                double *V = d.vk + idm * nn + mbase;
-                Real djl[NFJ * NFL], djk[NFJ * NFK], dil[NFI * NFL], dik[NFI * NFK];
+            nst += __popc(fin);
+            __syncwarp();
+            if (nst >= 32) {
+                lean_digest<LI, LJ, LK, LL, Real>(d, c, stage, stage_q, 32, ab_buf, lane);
+                __syncwarp();
+                const int rem = nst - 32;   // at most 31: move them to the front
+                if (lane < rem) {
 #pragma unroll
-                for (int b = 0; b < NFJ; ++b) {
-#pragma unroll
-                    for (int dd = 0; dd < NFL; ++dd) djl[b * NFL + dd] = Dm[(size_t)(aj + b) * nao + al + dd];
-#pragma unroll
-                    for (int cc = 0; cc < NFK; ++cc) djk[b * NFK + cc] = Dm[(size_t)(aj + b) * nao + ak + cc];
+                    for (int e = 0; e < NF; ++e) stage[e * LEAN_STAGE + lane] = stage[e * LEAN_STAGE + 32 + lane];
+                    stage_q[lane] = stage_q[32 + lane];
                 }
-#pragma unroll
-                for (int a = 0; a < NFI; ++a) {
-#pragma unroll
-                    for (int dd = 0; dd < NFL; ++dd) dil[a * NFL + dd] = Dm[(size_t)(ai + a) * nao + al + dd];
-#pragma unroll
-                    for (int cc = 0; cc < NFK; ++cc) dik[a * NFK + cc] = Dm[(size_t)(ai + a) * nao + ak + cc];
-                }
-#pragma unroll
-                for (int a = 0; a < NFI; ++a)
-#pragma unroll
-                    for (int cc = 0; cc < NFK; ++cc) {   // K[i a, k c] += E D[j b, l d]
-                        Real s = Real(0);
-#pragma unroll
-                        for (int b = 0; b < NFJ; ++b)
-#pragma unroll
-                            for (int dd = 0; dd < NFL; ++dd) s += acc[((a * NFJ + b) * NFK + cc) * NFL + dd] * djl[b * NFL + dd];
-                        warp_agg_add(vd ? V + (size_t)(ai + a) * nao + ak + cc : nullptr, fac * s, ab_buf, lane);
-                    }
-#pragma unroll
-                for (int a = 0; a < NFI; ++a)
-#pragma unroll
-                    for (int dd = 0; dd < NFL; ++dd) {   // K[i a, l d] += E D[j b, k c]
-                        Real s = Real(0);
-#pragma unroll
-                        for (int b = 0; b < NFJ; ++b)
-#pragma unroll
-                            for (int cc = 0; cc < NFK; ++cc) s += acc[((a * NFJ + b) * NFK + cc) * NFL + dd] * djk[b * NFK + cc];
-                        warp_agg_add(vd ? V + (size_t)(ai + a) * nao + al + dd : nullptr, fac * s, ab_buf, lane);
-                    }
-#pragma unroll
-                for (int b = 0; b < NFJ; ++b)
-#pragma unroll
-                    for (int cc = 0; cc < NFK; ++cc) {   // K[j b, k c] += E D[i a, l d]
-                        Real s = Real(0);
-#pragma unroll
-                        for (int a = 0; a < NFI; ++a)
-#pragma unroll
-                            for (int dd = 0; dd < NFL; ++dd) s += acc[((a * NFJ + b) * NFK + cc) * NFL + dd] * dil[a * NFL + dd];
-                        warp_agg_add(vd ? V + (size_t)(aj + b) * nao + ak + cc : nullptr, fac * s, ab_buf, lane);
-                    }
-#pragma unroll
-                for (int b = 0; b < NFJ; ++b)
-#pragma unroll
-                    for (int dd = 0; dd < NFL; ++dd) {   // K[j b, l d] += E D[i a, k c]
-                        Real s = Real(0);
-#pragma unroll
-                        for (int a = 0; a < NFI; ++a)
-#pragma unroll
-                            for (int cc = 0; cc < NFK; ++cc) s += acc[((a * NFJ + b) * NFK + cc) * NFL + dd] * dik[a * NFK + cc];
-                        warp_agg_add(vd ? V + (size_t)(aj + b) * nao + al + dd : nullptr, fac * s, ab_buf, lane);
-                    }
+                nst = rem;
+                __syncwarp();
             }
         }
     }
+    if (nst > 0) lean_digest<LI, LJ, LK, LL, Real>(d, c, stage, stage_q, nst, ab_buf, lane);
 }
 
 }  // namespace jk

@@ -183,21 +183,27 @@ int jk_probe_fma(double *out, int blocks, int iters, int fp32, void *stream);
 /* Allocation-free J/K build.  No counterpart in the reference: gpu4pyscf
  * always allocates its buffers with CuPy.
  *
- * For callers that must not allocate device memory during the call: code
- * recording a CUDA graph (an allocation breaks the capture), processes held
- * to a fixed device-memory budget after start-up, and hosts whose framework
- * owns every allocation.  Same arguments and results as jk_build (without
- * stats).  Every per-call buffer comes from one fixed device array of
+ * For callers that may not allocate device memory once they are running:
+ * processes held to a fixed device-memory budget after start-up, and host
+ * applications whose own framework owns every device allocation and forbids
+ * a library from calling cudaMalloc.  jk_build grows a per-optimizer
+ * workspace on demand; this entry point calls no cudaMalloc, cudaFree or
+ * allocating library routine.  Same arguments and results as jk_build
+ * (without stats), including the optimizer's launch variants and the
+ * precision modes.  Every per-call buffer comes from one fixed device array of
  * jk_noalloc_scratch_bytes() bytes (32 MiB) that every GPU loading this
  * library holds until the process exits; a call needs about
  * 8*nao^2*(2*n_dm + 2*n_dmk) bytes (n_dmk = 2*n_dm for hermi=0, else n_dm),
  * plus 4*nao^2*(n_dm + n_dmk) in mixed precision and 4*nbas^2 for the
  * screening table, and is rejected with JK_ERR_OVERFLOW above the limit.
  * The optimizer must come from jk_opt_create beforehand (that call does
- * allocate).  The first call on a device looks up the array's device
- * address; make that first call before any stream capture.  All calls share
- * the one array, so calls that overlap on the GPU (other streams, other
- * optimizers, other host threads) race: serialise them. */
+ * allocate).  The first call on a device also does a one-time set-up: it
+ * looks up the array's device address (cudaGetSymbolAddress) with that
+ * device current; make that first call before any stream capture.  Every
+ * call clears the parts of the array that must start at zero, and the array
+ * keeps the last call's contents otherwise.  All calls share the one array,
+ * so calls that overlap on the GPU (other streams, other optimizers, other
+ * host threads) race: serialise them. */
 int jk_noalloc_scratch_bytes(void);
 int jk_build_noalloc(jk_opt *opt, const double *dm, int n_dm, int nao, int hermi,
                      int with_j, int with_k, int precision, double split_thresh,

@@ -1,10 +1,12 @@
 """The allocation-free J/K entry point, called through the C ABI.
 
-jk_build_noalloc serves callers that cannot allocate device memory during
-the call (stream capture into a CUDA graph, a fixed device-memory budget, a
-host framework that owns all allocations).  Its results must equal those of
-jk_build, call after call, although every call reuses the same fixed
-scratch array.  This file is collected last on purpose.
+jk_build_noalloc serves callers that may not allocate device memory once
+they are running: a process held to a fixed device-memory budget after
+start-up, or a host application whose own framework owns every device
+allocation and forbids a library from calling cudaMalloc.  Its results must
+equal those of jk_build, call after call, although every call reuses the
+same fixed scratch array.  This file is collected last on purpose, so that a
+run stopping at the first failure has already run every other test.
 """
 import ctypes
 
@@ -30,11 +32,12 @@ def _setup(basis='syn-def2-svp'):
     return torch, lib, libjk, opt
 
 
-def _noalloc(torch, lib, libjk, opt, dms, hermi):
+def _noalloc(torch, lib, libjk, opt, dms, hermi, prec=None, split=0.):
+    prec = libjk.JK_PREC_FP64 if prec is None else prec
     vj = torch.full_like(dms, float('nan'))
     vk = torch.full_like(dms, float('nan'))
     err = lib.jk_build_noalloc(opt._handle, dms.data_ptr(), dms.shape[0], dms.shape[-1], hermi, 1, 1,
-                               libjk.JK_PREC_FP64, 0., vj.data_ptr(), vk.data_ptr(),
+                               prec, split, vj.data_ptr(), vk.data_ptr(),
                                torch.cuda.current_stream().cuda_stream)
     libjk.check(err, 'jk_build_noalloc')
     return vj, vk
@@ -55,6 +58,27 @@ def test_noalloc_matches_jk_build_twice(hermi):
         torch.cuda.synchronize()
         assert abs(vj - ref_j).max().item() < 1e-10, call
         assert abs(vk - ref_k).max().item() < 1e-10, call
+
+
+@pytest.mark.parametrize('precision', ['mixed', 'mixed-fp32roots'])
+def test_noalloc_mixed_matches_jk_build_twice(precision):
+    """Mixed FP32/FP64 builds through the allocation-free entry point agree
+    with jk_build's mixed builds (the same quartets in the same precision;
+    only the order of the FP64 atomic additions differs)."""
+    torch, lib, libjk, opt = _setup('syn-def2-tzvp')
+    rng = np.random.default_rng(12)
+    n = opt.sorted_mol.nao
+    opt.precision, opt.split_thresh = precision, 1e-4
+    for call in range(2):
+        d = rng.random((1, n, n)) - .4
+        d = d + d.transpose(0, 2, 1)
+        dms = torch.as_tensor(d, device='cuda')
+        ref_j, ref_k = opt._build(dms, 1, True, True)
+        vj, vk = _noalloc(torch, lib, libjk, opt, dms, 1, libjk.PRECISIONS[precision], 1e-4)
+        torch.cuda.synchronize()
+        assert abs(vj - ref_j).max().item() < 1e-10, call
+        assert abs(vk - ref_k).max().item() < 1e-10, call
+    opt.precision = 'fp64'
 
 
 def test_noalloc_rejects_oversize_request():
