@@ -7,15 +7,17 @@ Method (this project's own tables; nothing is taken from other code):
   weights come from the moments by the Chebyshev algorithm (ordinary moments
   -> three-term recurrence), then Golub-Welsch on the Jacobi matrix, all in
   80-digit mpmath arithmetic.
-* 0 <= T < T_asym(n): piecewise polynomials on intervals of width 2.  On each
-  interval the 2n functions (u_1..u_n, w_1..w_n) are interpolated at the 14
-  Chebyshev points and the interpolant is re-expanded, in high precision, in
-  monomials of x = T - centre (x in [-1, 1]), so the device evaluates 13
-  Horner steps per function.
-* The FP32 quartets use a second table on the same intervals with degree
+* 0 <= T < T_asym(n): piecewise polynomials on intervals of width 1/2.  On
+  each interval the 2n functions (u_1..u_n, w_1..w_n) are interpolated at
+  the 10 Chebyshev points and the interpolant is re-expanded, in high
+  precision, in monomials of x = T - centre (|x| <= 1/4), so the device
+  evaluates 9 Horner steps per function (max relative error 4e-16).  On
+  GB300 every FP64 instruction is precious and table loads are not: narrow
+  intervals trade table size (1.1 MB) for FMAs.
+* The FP32 quartets use a second table on intervals of width 2 with degree
   DEG_F = 8 (9 Chebyshev points), whose interpolation error (< 4e-9
-  relative) is below FP32 rounding; fewer coefficients mean fewer loads and
-  FMAs per root evaluation.
+  relative) is below FP32 rounding; it is staged in shared memory by the
+  FP32 kernels, so it stays small.
 * T >= T_asym(n): u_r = h_r^2 / T, w_r = W_r / sqrt(T), with h_r, W_r the
   positive nodes and weights of 2n-point Gauss-Hermite quadrature (the
   integral over [0, 1] extended to [0, inf)).  T_asym(n) = 40 + 6n is where
@@ -29,15 +31,15 @@ import sys
 import multiprocessing as mp_proc
 
 NMAX = 9
-DEG = 13
+DEG = 9
+INV_WIDTH = 2     # FP64 table: intervals of width 1 / INV_WIDTH
 DEG_F = 8
-WIDTH = 2
+WIDTH_F = 2       # FP32 table: intervals of width WIDTH_F
 DPS = 80
 
 
 def t_asym(n):
-    t = 40 + 6 * n
-    return t + (-t) % WIDTH
+    return 40 + 6 * n   # a multiple of both interval widths
 
 
 def _mp():
@@ -84,12 +86,12 @@ def hermite(mp, m):
 
 
 def fit_interval(args):
-    """Monomial coefficients [deg+1][2n] in x = T - centre on one interval."""
-    n, k = args[:2]
-    deg = args[2] if len(args) > 2 else DEG
+    """Monomial coefficients [deg+1][2n] in x = T - centre on interval k of
+    width `width`."""
+    n, k, deg, width = args
     mp = _mp()
-    a = mp.mpf(k * WIDTH)
-    half = mp.mpf(WIDTH) / 2
+    a = mp.mpf(k) * mp.mpf(width)
+    half = mp.mpf(width) / 2
     c = a + half
     N = deg + 1
     nodes = [mp.cos(mp.pi * (j + mp.mpf(1) / 2) / N) for j in range(N)]
@@ -128,16 +130,16 @@ def fit_interval(args):
 
 
 def check_interval(args):
-    """Max relative error of the double-precision table on one interval."""
-    n, k, coef = args[:3]
-    deg = args[3] if len(args) > 3 else DEG
+    """Max relative error of a table (coefficients rounded to double) on one
+    interval."""
+    n, k, coef, deg, width = args
     mp = _mp()
     worst = 0.
     for frac in (0.07, 0.31, 0.5, 0.77, 0.96):
-        T = k * WIDTH + frac * WIDTH
+        T = (k + frac) * width
         u, w = rys(mp, n, T)
         ref = [float(v) for v in u + w]
-        x = T - (k * WIDTH + WIDTH / 2)
+        x = T - (k + 0.5) * width
         for f in range(2 * n):
             acc = coef[deg][f]
             for i in range(deg - 1, -1, -1):
@@ -148,34 +150,41 @@ def check_interval(args):
 
 def main():
     mp = _mp()
-    jobs = [(n, k) for n in range(1, NMAX + 1) for k in range(t_asym(n) // WIDTH)]
+    w64 = 1. / INV_WIDTH
+    jobs = [(n, k, DEG, w64) for n in range(1, NMAX + 1) for k in range(t_asym(n) * INV_WIDTH)]
+    jobs_f = [(n, k, DEG_F, WIDTH_F) for n in range(1, NMAX + 1) for k in range(t_asym(n) // WIDTH_F)]
     ctx = mp_proc.get_context('spawn')
     with ctx.Pool(os.cpu_count()) as pool:
         res = pool.map(fit_interval, jobs, chunksize=4)
         table = {(n, k): c for n, k, c in res}
-        errs = pool.map(check_interval, [(n, k, table[(n, k)]) for n, k in jobs], chunksize=4)
-        res_f = pool.map(fit_interval, [(n, k, DEG_F) for n, k in jobs], chunksize=4)
+        errs = pool.map(check_interval, [(n, k, table[(n, k)], DEG, w64) for n, k, _, _ in jobs], chunksize=4)
+        res_f = pool.map(fit_interval, jobs_f, chunksize=4)
         table_f = {(n, k): c for n, k, c in res_f}
-        errs_f = pool.map(check_interval, [(n, k, table_f[(n, k)], DEG_F) for n, k in jobs], chunksize=4)
+        errs_f = pool.map(check_interval, [(n, k, table_f[(n, k)], DEG_F, WIDTH_F) for n, k, _, _ in jobs_f],
+                          chunksize=4)
     worst, worst_f = {}, {}
-    for (n, k), e, ef in zip(jobs, errs, errs_f):
+    for (n, k, _, _), e in zip(jobs, errs):
         worst[n] = max(worst.get(n, 0.), e)
-        worst_f[n] = max(worst_f.get(n, 0.), ef)
+    for (n, k, _, _), e in zip(jobs_f, errs_f):
+        worst_f[n] = max(worst_f.get(n, 0.), e)
     lines = []
     lines.append('// Generated by gen_rys_tables.py -- do not edit.')
     lines.append('// Rys roots/weights: piecewise degree-%d polynomials in x = T - centre on' % DEG)
-    lines.append('// intervals of width %d for T < T_asym(n) = 40 + 6n; Gauss-Hermite asymptote beyond.' % WIDTH)
+    lines.append('// intervals of width 1/%d for T < T_asym(n) = 40 + 6n; Gauss-Hermite asymptote beyond.' % INV_WIDTH)
     lines.append('// Max relative error of the double table vs 80-digit reference, per n:')
     for n in range(1, NMAX + 1):
         lines.append('//   n=%d: %.2e' % (n, worst[n]))
-    lines.append('// FP32 table (degree %d): max relative interpolation error per n (coefficients then rounded to float):' % DEG_F)
+    lines.append('// FP32 table (degree %d, intervals of width %d): max relative interpolation error per n '
+                 '(coefficients then rounded to float):' % (DEG_F, WIDTH_F))
     for n in range(1, NMAX + 1):
         lines.append('//   n=%d: %.2e' % (n, worst_f[n]))
     lines.append('#define RYS_NMAX %d' % NMAX)
     lines.append('#define RYS_DEG %d' % DEG)
+    lines.append('#define RYS_INV_WIDTH %d' % INV_WIDTH)
     lines.append('#define RYS_DEG_F %d' % DEG_F)
-    lines.append('#define RYS_WIDTH %d' % WIDTH)
-    nint = [0] + [t_asym(n) // WIDTH for n in range(1, NMAX + 1)]
+    lines.append('#define RYS_WIDTH_F %d' % WIDTH_F)
+    nint = [0] + [t_asym(n) * INV_WIDTH for n in range(1, NMAX + 1)]
+    nint_f = [0] + [t_asym(n) // WIDTH_F for n in range(1, NMAX + 1)]
     # offs[n] = first element of the block for n roots (offs[0] unused)
     offs = [0, 0]
     for n in range(1, NMAX):
@@ -194,14 +203,15 @@ def main():
     lines.append('};')
     offs_f = [0, 0]
     for n in range(1, NMAX):
-        offs_f.append(offs_f[-1] + nint[n] * (DEG_F + 1) * 2 * n)
-    total_f = offs_f[-1] + nint[NMAX] * (DEG_F + 1) * 2 * NMAX
+        offs_f.append(offs_f[-1] + nint_f[n] * (DEG_F + 1) * 2 * n)
+    total_f = offs_f[-1] + nint_f[NMAX] * (DEG_F + 1) * 2 * NMAX
     lines.append('#define RYS_TABLE_F_SIZE %d' % total_f)
+    lines.append('static const int rys_nint_f_host[RYS_NMAX + 1] = {%s};' % ', '.join(map(str, nint_f)))
     lines.append('static const int rys_offset_f_host[RYS_NMAX + 1] = {%s};' % ', '.join(map(str, offs_f)))
     lines.append('// FP32 layout per n: [interval][power 0..DEG_F][u_1..u_n, w_1..w_n]')
     lines.append('static const float rys_coef_f_host[RYS_TABLE_F_SIZE] = {')
     for n in range(1, NMAX + 1):
-        for k in range(nint[n]):
+        for k in range(nint_f[n]):
             c = table_f[(n, k)]
             for i in range(DEG_F + 1):
                 lines.append('  ' + ', '.join('%.9ef' % v for v in c[i]) + ',')

@@ -49,7 +49,7 @@ struct EngineDev {
     const ShellDev *shells;
     // primitive-pair data, one entry per primitive pair of every kept shell pair
     const d4 *pp_a;        // {p, Px, Py, Pz}
-    const d4 *pp_b;        // {PAx, PAy, PAz, Kab*ci*cj}   (A = first shell)
+    const d4 *pp_b;        // {PAx, PAy, PAz, sqrt(2 pi^(5/2)) Kab ci cj / p}   (A = first shell)
     const double *pp_ip;      // 1/p
     const float4 *pp_af;      // float copies for the FP32 quartets
     const float4 *pp_bf;

@@ -426,6 +426,7 @@ struct PrimPairHost {
 // it), are left out -- tight primitives on different atoms decay to nothing
 // -- but the largest one is always kept.  Returns the number added.
 constexpr double PRIM_PRUNE = 1e-18;
+const double SQRT_TWO_PI25 = std::sqrt(2. * std::pow(M_PI, 2.5));
 
 inline double prim_weight(double a, double b, double ca, double cb, double AB2) {
     double p = a + b;
@@ -452,7 +453,10 @@ int add_prim_pairs(const jk_opt *o, int i, int j, PrimPairHost &pp, bool prune =
             double ca = o->coefs_h[o->prim0_h[i] + pa], cb = o->coefs_h[o->prim0_h[j] + pb];
             if (prune && pa * B.nprim + pb != kmax && prim_weight(a, b, ca, cb, AB2) < PRIM_PRUNE) continue;
             double p = a + b;
-            double K = std::exp(-a * b / p * AB2) * ca * cb;
+            // K_ab c_a c_b / p times sqrt(2 pi^(5/2)): the product of a bra's
+            // and a ket's value times 1/sqrt(p+q) is the ERI prefactor
+            // 2 pi^(5/2) K_ab K_cd c_a c_b c_c c_d / (p q sqrt(p+q))
+            double K = std::exp(-a * b / p * AB2) * ca * cb * SQRT_TWO_PI25 / p;
             double Px = (a * A.x + b * B.x) / p, Py = (a * A.y + b * B.y) / p, Pz = (a * A.z + b * B.z) / p;
             pp.a.push_back(d4{p, Px, Py, Pz});
             pp.b.push_back(d4{Px - A.x, Py - A.y, Pz - A.z, K});

@@ -7,8 +7,6 @@ namespace jk {
 
 enum { MODE_JK = 0, MODE_DIAG = 1 };
 
-constexpr double TWO_PI25 = 34.98683665524972497;  // 2 * pi^(5/2)
-
 __device__ __forceinline__ void cart_xyz(int l, int c, int &x, int &y, int &z) {
     int idx = 0;
     for (int lx = l; lx >= 0; --lx)
@@ -242,7 +240,7 @@ rys_class_kernel(EngineDev d, ClassDev c, int ntiles_static)
                     double ipq = rs * rs;
                     double PQx = a1.y - a2.y, PQy = a1.z - a2.z, PQz = a1.w - a2.w;
                     double T = p * q * ipq * (PQx * PQx + PQy * PQy + PQz * PQz);
-                    double pref = TWO_PI25 * b1.w * b2.w * ip1 * ip2 * rs * d.op_scale;
+                    double pref = b1.w * b2.w * rs * d.op_scale;
                     double u[NR], w[NR];
                     rys_roots_rs<NR>(T, p * q * ipq, d.omega2, d.rys_coef, u, w);
 #pragma unroll
@@ -261,7 +259,7 @@ rys_class_kernel(EngineDev d, ClassDev c, int ntiles_static)
                     float ipq = rs * rs;
                     float PQx = a1.y - a2.y, PQy = a1.z - a2.z, PQz = a1.w - a2.w;
                     float T = p * q * ipq * (PQx * PQx + PQy * PQy + PQz * PQz);
-                    float pref = (float)TWO_PI25 * b1.w * b2.w * ip1 * ip2 * rs * d.op_scale_f;
+                    float pref = b1.w * b2.w * rs * d.op_scale_f;
                     float u[NR], w[NR];
                     rys_roots_rs_f<NR>(T, p * q * ipq, d.omega2_f, d.rys_coef_f, u, w, d.fp32_asym);
 #pragma unroll

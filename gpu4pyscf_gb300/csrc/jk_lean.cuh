@@ -169,8 +169,8 @@ __device__ __forceinline__ void lean_digest(const EngineDev &d, const ClassDev &
     const size_t nn = (size_t)d.ntot;
     const size_t mbase = (size_t)__ldg(d.mol_base + mol);
     const int ndm_m = d.mol_ndm ? __ldg(d.mol_ndm + mol) : d.n_dm;
-    const Real fac = Real((pij.x == pij.y ? .5 : 1.) * (pkl.x == pkl.y ? .5 : 1.) *
-                          (c.same && q.x == q.y ? .5 : 1.));
+    const Real fac = (sizeof(Real) == 8 ? Real(d.op_scale) : Real(d.op_scale_f)) *
+                     Real((pij.x == pij.y ? .5f : 1.f) * (pkl.x == pkl.y ? .5f : 1.f) * (c.same && q.x == q.y ? .5f : 1.f));
     const int ai = A.ao, aj = d.shells[pij.y].ao;
     const int ak = d.shells[pkl.x].ao, al = d.shells[pkl.y].ao;
     const Real *E = st + lane;   // element e of this lane's quartet: E[e * LEAN_STAGE]
@@ -432,8 +432,8 @@ rys_lean_kernel(EngineDev d, ClassDev c, int unused)
                 rys_roots_rs_f<NR, true>(T, rho, d.omega2_f, s_rys, u, w, d.fp32_asym);
             }
             const Real ipq = rs * rs;
-            const Real pref = Real(34.98683665524972497) * Kb * Kk * ipb * ipk * rs *
-                              (sizeof(Real) == 8 ? Real(d.op_scale) : Real(d.op_scale_f));
+            // the operator scale is applied once per quartet, at digestion
+            const Real pref = Kb * Kk * rs;
             const Real qpq = q * ipq, ppq = p * ipq;
             const Real h2p = Real(0.5) * ipb, h2q = Real(0.5) * ipk, h2pq = Real(0.5) * ipq;
 #pragma unroll

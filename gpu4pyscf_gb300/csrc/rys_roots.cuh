@@ -1,10 +1,12 @@
 // Rys roots and weights on the device from the tables of gen_rys_tables.py.
 //
-// T < 40 + 6n: Horner evaluation of the interval polynomial (degree 13 in
-// x = T - centre, intervals of width 2; degree 8 for the FP32 table), for the
-// roots u_r = t_r^2 and the weights w_r (sum_r w_r = F_0(T)).
+// T < 40 + 6n: Horner evaluation of the interval polynomial, for the roots
+// u_r = t_r^2 and the weights w_r (sum_r w_r = F_0(T)): degree 9 in
+// x = T - centre on intervals of width 1/2 for the FP64 table, degree 8 on
+// intervals of width 2 for the FP32 table.
 // T >= 40 + 6n: u_r = h_r^2 / T, w_r = W_r / sqrt(T) from 2n-point
-// Gauss-Hermite quadrature, always evaluated in FP64.
+// Gauss-Hermite quadrature, evaluated in FP64 (or FP32 on request for the
+// FP32 quartets).
 #pragma once
 #include "rys_tables.inc"
 
@@ -13,13 +15,25 @@ namespace jk {
 __constant__ double c_rys_asym_x2[RYS_ASYM_SIZE] = {RYS_ASYM_X2_LIST};
 __constant__ double c_rys_asym_w[RYS_ASYM_SIZE] = {RYS_ASYM_W_LIST};
 
-__host__ __device__ constexpr int rys_nint(int n) { return (40 + 6 * n) / RYS_WIDTH; }
+static_assert(RYS_INV_WIDTH == 2, "the FP64 interval index below assumes intervals of width 1/2");
+
+__host__ __device__ constexpr int rys_tmax(int n) { return 40 + 6 * n; }
+__host__ __device__ constexpr int rys_nint(int n) { return rys_tmax(n) * RYS_INV_WIDTH; }
 __host__ __device__ constexpr int rys_off(int n) {
     return n <= 1 ? 0 : rys_off(n - 1) + rys_nint(n - 1) * (RYS_DEG + 1) * 2 * (n - 1);
 }
-// the FP32 table: same intervals, degree RYS_DEG_F
+// the FP32 table: its own intervals and degree
+__host__ __device__ constexpr int rys_nint_f(int n) { return rys_tmax(n) / RYS_WIDTH_F; }
 __host__ __device__ constexpr int rys_off_f(int n) {
-    return n <= 1 ? 0 : rys_off_f(n - 1) + rys_nint(n - 1) * (RYS_DEG_F + 1) * 2 * (n - 1);
+    return n <= 1 ? 0 : rys_off_f(n - 1) + rys_nint_f(n - 1) * (RYS_DEG_F + 1) * 2 * (n - 1);
+}
+
+// High 32 bits of the double of a small positive integer v (its low word is
+// zero): sign 0, biased exponent, the top 20 bits of the fraction.
+__host__ __device__ constexpr int dbl_hi_of_int(int v) {
+    int e = 0;
+    while ((2 << e) <= v) ++e;
+    return ((1023 + e) << 20) | ((v - (1 << e)) << (20 - e));
 }
 
 template <int NR>
@@ -34,16 +48,33 @@ __device__ __forceinline__ void rys_asym(double T, double *u, double *w) {
     }
 }
 
-// FP64 roots: table in double
+// FP64 roots: table in double.  The branch on T, the interval index
+// k = floor(2T) and the interval centre (2k+1)/4 come from the bits of T with
+// integer operations, leaving one FP64 subtraction before the Horner steps:
+// on GB300 FP64 instructions are the scarce resource and the integer pipes
+// idle.  T >= 0 (a -0 lands in interval 0); NaN takes the asymptote branch
+// (no table access).
 template <int NR>
 __device__ __forceinline__ void rys_roots(double T, const double *__restrict__ coef, double *u, double *w) {
     static_assert(NR <= RYS_NMAX, "too many roots");
-    if (!(T < 2.0 * rys_nint(NR))) {  // NaN also takes this branch (no table access)
+    const int hi = __double2hiint(T);
+    if (hi >= dbl_hi_of_int(rys_tmax(NR))) {   // T >= T_asym(n), or NaN
         rys_asym<NR>(T, u, w);
         return;
     }
-    int k = (int)(T * 0.5);
-    double x = T - (2 * k + 1);
+    // T = m 2^(e-20) with m the 21-bit significand of the high word; the low
+    // word cannot change floor(2T) = m >> (19 - e) (zero for T < 1/2)
+    const int e = ((hi >> 20) & 0x7ff) - 1023;
+    const int m = (hi & 0xfffff) | 0x100000;
+    const int sh = 19 - e;
+    const int k = sh > 20 ? 0 : (m >> sh);
+    // centre (2k+1)/4 as a double built from its bits (an odd integer n
+    // below 2^9 times 2^-2: exponent b-2 for its top bit b, fraction bits in
+    // the high word)
+    const int n = 2 * k + 1;
+    const int b = 31 - __clz(n);
+    const double centre = __hiloint2double(((1023 + b - 2) << 20) | ((n - (1 << b)) << (20 - b)), 0);
+    const double x = T - centre;
     const double *c = coef + rys_off(NR) + k * (RYS_DEG + 1) * 2 * NR;
     double a[2 * NR];
 #pragma unroll
@@ -61,13 +92,13 @@ __device__ __forceinline__ void rys_roots(double T, const double *__restrict__ c
 // evaluating different intervals read different banks (every class has
 // fewer than 32 intervals per root count).
 __host__ __device__ constexpr int rys_f_stride(int n) { return ((RYS_DEG_F + 1) * 2 * n) | 1; }
-__host__ __device__ constexpr int rys_f_smem(int n) { return rys_nint(n) * rys_f_stride(n); }
+__host__ __device__ constexpr int rys_f_smem(int n) { return rys_nint_f(n) * rys_f_stride(n); }
 
 template <int NR>
 __device__ __forceinline__ void rys_stage_f(const float *__restrict__ coef, float *s, int tid, int nthreads) {
     constexpr int per = (RYS_DEG_F + 1) * 2 * NR;
     const float *src = coef + rys_off_f(NR);
-    for (int e = tid; e < rys_nint(NR) * per; e += nthreads) s[(e / per) * rys_f_stride(NR) + e % per] = __ldg(src + e);
+    for (int e = tid; e < rys_nint_f(NR) * per; e += nthreads) s[(e / per) * rys_f_stride(NR) + e % per] = __ldg(src + e);
 }
 
 // FP32 roots: table in float; the asymptote in FP64 (or in FP32 when
@@ -77,7 +108,7 @@ __device__ __forceinline__ void rys_stage_f(const float *__restrict__ coef, floa
 template <int NR, bool SMEM = false>
 __device__ __forceinline__ void rys_roots_f(float T, const float *__restrict__ coef, float *u, float *w,
                                             int asym32 = 0) {
-    if (!(T < 2.f * rys_nint(NR))) {
+    if (!(T < (float)rys_tmax(NR))) {
         if (asym32) {
             const float rs = rsqrtf(T);
             const float it = rs * rs;
@@ -95,6 +126,7 @@ __device__ __forceinline__ void rys_roots_f(float T, const float *__restrict__ c
         for (int r = 0; r < NR; ++r) { u[r] = (float)ud[r]; w[r] = (float)wd[r]; }
         return;
     }
+    static_assert(RYS_WIDTH_F == 2, "FP32 intervals of width 2");
     int k = (int)(T * 0.5f);
     float x = T - (float)(2 * k + 1);
     float a[2 * NR];
@@ -128,13 +160,16 @@ __device__ __forceinline__ void rys_roots_f(float T, const float *__restrict__ c
 template <int NR>
 __device__ __forceinline__ void rys_roots_rs(double T, double rho, double omega2,
                                              const double *__restrict__ coef, double *u, double *w) {
-    const double theta = omega2 > 0. ? omega2 / (omega2 + rho) : 1.;
-    rys_roots<NR>(T * theta, coef, u, w);
-    if (omega2 > 0.) {
-        const double st = sqrt(theta);
-#pragma unroll
-        for (int r = 0; r < NR; ++r) { u[r] *= theta; w[r] *= st; }
+    // omega2 >= 0; its high word tells 0 from positive without an FP64 compare
+    if (__double2hiint(omega2) <= 0) {
+        rys_roots<NR>(T, coef, u, w);
+        return;
     }
+    const double theta = omega2 / (omega2 + rho);
+    rys_roots<NR>(T * theta, coef, u, w);
+    const double st = sqrt(theta);
+#pragma unroll
+    for (int r = 0; r < NR; ++r) { u[r] *= theta; w[r] *= st; }
 }
 
 template <int NR, bool SMEM = false>
