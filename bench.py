@@ -405,33 +405,78 @@ def kernel_family(li, lj, lk, ll):
 NCU_DRAM_BYTES = {('c30', '(21|11)'): 3100160, ('c30', '(11|10)'): 3365376}
 
 
+def train_guess_model(basis, nbase, nconf, epochs, seed=0):
+    """A learned-guess network trained on this engine's converged densities
+    of nbase x nconf seeded conformers (8-20 heavy atoms) in ``basis``
+    (batched SCFs); returns (model, info)."""
+    from gpu4pyscf_gb300.scf import learned_guess as lg
+    t0 = time.perf_counter()
+    confsets = lg.make_conformers(nbase, nconf, basis, seed)
+    nblock = max(b - a for cs in confsets for (a, b) in lg.block_slices(cs[0]))
+    data = lg.generate_batched(confsets, 0)
+    t_gen = time.perf_counter() - t0
+    model = lg.train(data, nblock, epochs=epochs, lr=2e-3, seed=seed)
+    return model, {'basis': basis, 'train_conformers': len(data), 'generate_s': t_gen,
+                   'train_s': time.perf_counter() - t0 - t_gen, 'epochs': epochs,
+                   'final_train_loss': model.loss_history[-1]}
+
+
 def run_scf(args):
-    """Full RHF to 1e-8 Ha with DIIS on one molecule: FP64 J/K vs mixed
-    J/K (split args.split), both from the SAD guess."""
+    """Full RHF to 1e-8 Ha with DIIS on one molecule: FP64 J/K from the SAD
+    guess against mixed J/K (split args.split) from the SAD guess and, with
+    --guess learned, from the learned guess (a network trained first on
+    converged densities of small conformers in the same basis)."""
     import torch
     from gpu4pyscf_gb300.scf import hf
     mol = make_mol(args.config)
+    model, model_info = None, None
+    arms = [('fp64', 'sad'), ('mixed', 'sad')]
+    if args.guess == 'learned':
+        model, model_info = train_guess_model(CONFIGS[args.config]['basis'], args.guess_bases,
+                                              args.guess_conformers, args.guess_epochs)
+        arms.append(('mixed', 'learned'))
     rows = []
-    for prec in ('fp64', 'mixed'):
+    for prec, g in arms:
         mf = hf.RHF(mol)
         mf.conv_tol = 1e-8
-        mf.max_cycle = 60
+        mf.max_cycle = 80
         mf.precision = prec
         mf.split_thresh = args.split
         mf.verbose = True          # per-cycle progress on stderr
-        print('== %s' % prec, file=sys.stderr, flush=True)
+        print('== %s %s' % (prec, g), file=sys.stderr, flush=True)
         torch.cuda.synchronize()
         t0 = time.perf_counter()
+        if g == 'learned':
+            mf.init_guess, mf.guess_model = 'learned', model
         e = mf.kernel()
         torch.cuda.synchronize()
-        rows.append({'precision': prec, 'e_tot': e, 'cycles': mf.cycles, 'converged': mf.converged,
+        rows.append({'precision': prec, 'guess': g, 'e_tot': e, 'cycles': mf.cycles, 'converged': mf.converged,
                      'wall_s': time.perf_counter() - t0})
-    line = {'metric': 'scf_seconds_to_1e-8', 'value': rows[1]['wall_s'], 'unit': 's', 'n_gpus': 1,
+    last = rows[-1]
+    line = {'metric': 'scf_seconds_to_1e-8', 'value': last['wall_s'], 'unit': 's', 'n_gpus': 1,
             'higher_is_better': False, 'dtype': 'f64/mixed', 'data': 'synthetic',
             'config': {'workload': CONFIGS[args.config]['workload'], 'nao_user': mol.nao, 'natm': mol.natm,
-                       'split': args.split, 'guess': 'SAD'},
-            'runs': rows, 'dE_mixed_vs_fp64': rows[1]['e_tot'] - rows[0]['e_tot'],
-            'speedup_mixed_vs_fp64': rows[0]['wall_s'] / rows[1]['wall_s']}
+                       'split': args.split},
+            'runs': rows, 'dE_vs_fp64_sad': [r['e_tot'] - rows[0]['e_tot'] for r in rows],
+            'speedup_vs_fp64_sad': [rows[0]['wall_s'] / r['wall_s'] for r in rows],
+            'guess_model': model_info}
+    print(json.dumps(line))
+
+
+def run_guess(args):
+    """bench.py --mode guess: the learned initial guess at the scale of the
+    workload (seeded conformers of 8-20 heavy-atom C/N/O/H molecules,
+    syn-def2-svp; --guess-bases x --guess-conformers, the last
+    --guess-holdout of each base held out), trained on the engine's
+    converged FP64 densities; SCF cycles to 1e-8 Ha and energies of the
+    held-out conformers from SAD and from the learned guess."""
+    from gpu4pyscf_gb300.scf import learned_guess as lg
+    res, _ = lg.run(args.guess_bases, args.guess_conformers, args.guess_holdout, 'syn-def2-svp',
+                    args.guess_epochs, batched=True)
+    res = {k: v for k, v in res.items() if k != 'rows'}
+    line = {'metric': 'scf_cycles_learned_vs_sad', 'value': res['mean_cycles_learned'], 'unit': 'cycles',
+            'n_gpus': 1, 'higher_is_better': False, 'dtype': 'f64 (SCF), f32 (network)', 'data': 'synthetic',
+            'config': {'workload': res['workload']}, 'result': res}
     print(json.dumps(line))
 
 
@@ -740,9 +785,16 @@ def main():
     ap.add_argument('--ref-seconds', type=float, default=20.)
     ap.add_argument('--no-cpu', action='store_true')
     ap.add_argument('--no-batch', action='store_true')
-    ap.add_argument('--mode', default='jk', choices=['jk', 'scf', 'dense'],
+    ap.add_argument('--mode', default='jk', choices=['jk', 'scf', 'dense', 'guess'],
                     help='jk: the J/K benchmark line; scf: full RHF of --config (e.g. c120); '
-                         'dense: FP64 vs mixed J/K of a dense SCF density of --config')
+                         'dense: FP64 vs mixed J/K of a dense SCF density of --config; '
+                         'guess: the learned initial guess against SAD')
+    ap.add_argument('--guess', default='sad', choices=['sad', 'learned'],
+                    help='--mode scf: add a mixed-precision run from the learned guess')
+    ap.add_argument('--guess-bases', type=int, default=40)
+    ap.add_argument('--guess-conformers', type=int, default=50)
+    ap.add_argument('--guess-holdout', type=int, default=5)
+    ap.add_argument('--guess-epochs', type=int, default=200)
     args = ap.parse_args()
     if args.impl == 'reference':
         run_reference(args)
@@ -750,6 +802,8 @@ def main():
         run_scf(args)
     elif args.mode == 'dense':
         run_dense(args)
+    elif args.mode == 'guess':
+        run_guess(args)
     else:
         run_gpu(args)
 

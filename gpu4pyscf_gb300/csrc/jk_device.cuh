@@ -21,7 +21,10 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
-#define JK_LMAX 3
+// highest angular momentum of the engine (g); the templated kernels cover
+// classes up to f, classes with a g shell run the generic kernel
+#define JK_LMAX 4
+#define JK_LMAX_TEMPLATED 3
 #define JK_THREADS 256
 #define JK_SMEM_CAP (100 * 1024)
 
@@ -65,6 +68,14 @@ struct EngineDev {
     double *vk;               // K accumulator
     float *qout;              // Schwarz mode output (per pair)
     unsigned long long *counters;  // per class: [quartets, prim quartets]
+    // launch sizing from the optimizer's history: quartets each class launch
+    // (index class_id) computed in the previous build (null: none) and the
+    // counts of this build
+    const unsigned long long *qprev;
+    unsigned long long *qnow;
+    // deterministic accumulation (non-null when enabled): J and K elements
+    // as pairs of 64-bit fixed-point sums [2 * element] (see jk_add)
+    unsigned long long *vj_fx, *vk_fx;
     int nbas, nao, n_dm, n_dmk;
     // densities and J/K are stored per molecule as packed square blocks:
     // element (a, b) of molecule m in density idm sits at
@@ -104,27 +115,52 @@ struct ClassDev {
     // SPLIT_ALL every one, SPLIT_HIGH those whose bound reaches the split
     // (FP64 part of a mixed build), SPLIT_LOW those below it (FP32 part)
     int split_mode;
+    int li, lj, lk, ll;       // angular momenta of the class (read by the generic kernel)
 };
 
 enum { SPLIT_ALL = 0, SPLIT_HIGH = 1, SPLIT_LOW = 2 };
 
 // Screening of (bra, ket) of a class: q_ij q_kl times the largest of the six
 // density blocks the quartet touches against the cutoff
-// (gpu4pyscf/lib/gvhf-rys/create_tasks.cu:152-162).  In a mixed build the
-// same bound, the quartet's own, decides its precision: FP64 when it reaches
-// the split threshold, FP32 below it.
+// (gpu4pyscf/lib/gvhf-rys/create_tasks.cu:152-162).  A J-only build needs
+// only the two Coulomb blocks D_ij and D_kl (the screening of the
+// reference's J engine), which drops far more quartets of a sparse density.
+// In a mixed build the same bound, the quartet's own, decides its
+// precision: FP64 when it reaches the split threshold, FP32 below it.
 __device__ __forceinline__ bool pair_passes(const EngineDev &d, const ClassDev &c, int bra, int ket) {
     const int2 pij = c.bra.ij[bra], pkl = c.ket.ij[ket];
     const float *dc = d.dm_cond;
     const int nb = d.nbas;
-    float dmax = fmaxf(fmaxf(__ldg(dc + pij.x * nb + pij.y), __ldg(dc + pkl.x * nb + pkl.y)),
-                       fmaxf(fmaxf(__ldg(dc + pij.x * nb + pkl.x), __ldg(dc + pij.x * nb + pkl.y)),
-                             fmaxf(__ldg(dc + pij.y * nb + pkl.x), __ldg(dc + pij.y * nb + pkl.y))));
+    float dmax = fmaxf(__ldg(dc + pij.x * nb + pij.y), __ldg(dc + pkl.x * nb + pkl.y));
+    if (d.with_k)
+        dmax = fmaxf(dmax, fmaxf(fmaxf(__ldg(dc + pij.x * nb + pkl.x), __ldg(dc + pij.x * nb + pkl.y)),
+                                 fmaxf(__ldg(dc + pij.y * nb + pkl.x), __ldg(dc + pij.y * nb + pkl.y))));
     const float v = __ldg(c.bra.logq + bra) + __ldg(c.ket.logq + ket) + dmax;
     if (!(v >= d.log_cut)) return false;
     if (c.split_mode == SPLIT_HIGH) return v >= d.log_split;
     if (c.split_mode == SPLIT_LOW) return v < d.log_split;
     return true;
+}
+
+// Adds v to J (isk false) or K element *addr.  Default: one FP64 atomic.
+// Deterministic mode: v = a 2^-24 + b 2^-56 (a = rint(v 2^24), b the
+// rounded remainder, |b| <= 2^31) goes into two 64-bit integer sums per
+// element; integer addition does not depend on the order of the atomics, so
+// the result is bitwise reproducible (rounding error <= 2^-57 per
+// contribution).
+#define JK_FX_HI 0x1p24
+#define JK_FX_LO 0x1p56
+__device__ __forceinline__ void jk_add(const EngineDev &d, bool isk, double *addr, double v) {
+    unsigned long long *fx = isk ? d.vk_fx : d.vj_fx;
+    if (fx == nullptr) {
+        atomicAdd(addr, v);
+        return;
+    }
+    const size_t off = addr - (isk ? d.vk : d.vj);
+    const double a = rint(v * JK_FX_HI);
+    const double r = fma(-a, 1. / JK_FX_HI, v);
+    atomicAdd(fx + 2 * off, (unsigned long long)__double2ll_rn(a));
+    atomicAdd(fx + 2 * off + 1, (unsigned long long)__double2ll_rn(r * JK_FX_LO));
 }
 
 // kets per work unit: a range [ket_begin[x], ket_end[x]) is cut into units
@@ -158,6 +194,12 @@ __device__ __forceinline__ void unit_at_warp(const ClassDev &c, int w, int lane,
 // quartets each.
 #define JK_MIN_UNITS 8
 
+// With the previous build's count of a launch's quartets at hand, a launch
+// keeps enough warps (blocks) for about JK_Q_PER_LANE quartets per lane (per
+// slot): classes whose kets mostly fail the density screening otherwise
+// spread a few quartets over thousands of warps.
+#define JK_Q_PER_LANE 4
+
 __host__ __device__ constexpr int ncart(int l) { return (l + 1) * (l + 2) / 2; }
 
 // Threads per quartet and quartets per block for a class.
@@ -170,9 +212,12 @@ struct ClassShape {
     static constexpr int GSKL = (LK + 1) * (LL + 1);
     static constexpr int GS = (LI + 1) * (LJ + 1) * GSKL;   // 2D integrals per (root, axis)
     static constexpr int NSC = 20;                            // per-quartet scalars
+    // per (quartet, root): u, w * prefactor and the axis-independent
+    // recurrence coefficients b00, b10, b01, u q/(p+q), u p/(p+q)
+    static constexpr int NRW = 7;
     __host__ __device__ static constexpr int g_bytes(int qb) { return qb * NR * 3 * GS * (int)sizeof(Real); }
     __host__ __device__ static constexpr int e_bytes(int qb) { return qb * NF * (int)sizeof(Real); }
-    __host__ __device__ static constexpr int aux_bytes(int qb) { return qb * (NR * 2 + NSC) * (int)sizeof(Real); }
+    __host__ __device__ static constexpr int aux_bytes(int qb) { return qb * (NR * NRW + NSC) * (int)sizeof(Real); }
     __host__ __device__ static constexpr int smem_of(int g) {
         return (g_bytes(JK_THREADS / g) > e_bytes(JK_THREADS / g) ? g_bytes(JK_THREADS / g) : e_bytes(JK_THREADS / g))
                + aux_bytes(JK_THREADS / g);

@@ -58,6 +58,7 @@ void init_registry() {
     register_bra_class_7(g_tab);
     register_bra_class_8(g_tab);
     register_bra_class_9(g_tab);
+    register_generic(g_tab);
 }
 
 template <typename T>
@@ -265,6 +266,12 @@ __global__ void scan_kernel(const ScanJob *jobs) {
     if (threadIdx.x == 0) jb.off[jb.n] = carry;
 }
 
+// fixed-point pairs (a, b) of the deterministic mode -> a 2^-24 + b 2^-56
+__global__ void fx_to_double_kernel(const unsigned long long *fx, size_t n, double *out) {
+    for (size_t x = blockIdx.x * (size_t)blockDim.x + threadIdx.x; x < n; x += (size_t)gridDim.x * blockDim.x)
+        out[x] = (double)(long long)fx[2 * x] * (1. / JK_FX_HI) + (double)(long long)fx[2 * x + 1] * (1. / JK_FX_LO);
+}
+
 __global__ void epilogue_kernel(const double *jt, const double *kt, int n_dm, Layout L, int hermi,
                                 int with_j, int with_k, double *vj, double *vk) {
     const size_t nn = (size_t)L.ntot;
@@ -340,8 +347,17 @@ struct jk_opt {
     float *dm_cond = nullptr, *dm_max = nullptr;
     int ws_ndm = 0;
     double *dmj = nullptr, *dmk = nullptr, *jt = nullptr, *kt = nullptr;
+    // deterministic accumulation: fixed-point sums of J and K (see jk_add)
+    bool det = false;
+    int fx_ndm = 0;
+    unsigned long long *jfx = nullptr, *kfx = nullptr;
     float *dmj_f = nullptr, *dmk_f = nullptr;
     unsigned long long *counters = nullptr;
+    // per-launch quartet counts of the last two builds (launch sizing from
+    // history); qhist_cur selects the half the next build writes
+    unsigned long long *qhist = nullptr;
+    int qhist_cur = 0;
+    bool qhist_valid = false;
     int *work = nullptr;                 // [2 passes][NQCLASS][2 precisions] unit counters of the class launches
     std::vector<void *> owned;
     // side streams: class kernels of one build run concurrently on them,
@@ -478,15 +494,25 @@ int launch_class(const void *func, int grid, int smem, const EngineDev &d, const
     return 0;
 }
 
+// Dynamic shared memory limit of every kernel: the largest any class
+// launching it needs (the generic kernel serves several classes).
 int set_smem_attrs() {
+    std::vector<std::pair<const void *, int>> need;
+    auto add = [&](const void *k, int bytes) {
+        if (!k) return;
+        for (auto &p : need)
+            if (p.first == k) { p.second = std::max(p.second, bytes); return; }
+        need.emplace_back(k, bytes);
+    };
     for (int q = 0; q < NQCLASS; ++q) {
         const ClassEntry &e = g_tab[q];
-        if (e.k64) CK(cudaFuncSetAttribute(e.k64, cudaFuncAttributeMaxDynamicSharedMemorySize, e.smem64));
-        if (e.k32) CK(cudaFuncSetAttribute(e.k32, cudaFuncAttributeMaxDynamicSharedMemorySize, e.smem32));
-        if (e.kdiag) CK(cudaFuncSetAttribute(e.kdiag, cudaFuncAttributeMaxDynamicSharedMemorySize, e.smemdiag));
-        if (e.k64_alt) CK(cudaFuncSetAttribute(e.k64_alt, cudaFuncAttributeMaxDynamicSharedMemorySize, e.smem64_alt));
-        if (e.k32_alt) CK(cudaFuncSetAttribute(e.k32_alt, cudaFuncAttributeMaxDynamicSharedMemorySize, e.smem32_alt));
+        add(e.k64, e.smem64);
+        add(e.k32, e.smem32);
+        add(e.kdiag, e.smemdiag);
+        add(e.k64_alt, e.smem64_alt);
+        add(e.k32_alt, e.smem32_alt);
     }
+    for (auto &p : need) CK(cudaFuncSetAttribute(p.first, cudaFuncAttributeMaxDynamicSharedMemorySize, p.second));
     return 0;
 }
 
@@ -635,7 +661,7 @@ static int create_impl(const int32_t *atm, int natm, const int32_t *bas, int nba
         const int32_t *b = bas + 8 * i;
         int ia = b[0], l = b[1], np = b[2], nctr = b[3], pe = b[5], pc = b[6];
         if (ia < 0 || ia >= natm) return bail(fail(JK_ERR_ARG, "shell atom index out of range"));
-        if (l < 0 || l > JK_LMAX) return bail(fail(JK_ERR_LMAX, "shell angular momentum above the GPU limit (f)"));
+        if (l < 0 || l > JK_LMAX) return bail(fail(JK_ERR_LMAX, "shell angular momentum above the GPU limit (g)"));
         if (nctr != 1) return bail(fail(JK_ERR_ARG, "sorted basis must have one contraction per shell"));
         if (np <= 0 || pe < 0 || pc < 0 || pe + np > nenv || pc + np > nenv)
             return bail(fail(JK_ERR_ARG, "shell primitive data out of range"));
@@ -736,6 +762,8 @@ static int create_impl(const int32_t *atm, int natm, const int32_t *bas, int nba
             c.bra.prim_cnt = c.ket.prim_cnt = dpc[pc];
             c.same = 1;
             c.class_id = quartet_class(pc, pc);
+            c.li = c.lk = pc_li(pc);
+            c.lj = c.ll = pc_lj(pc);
             d.qout = dq[pc];
             int ntiles = (n + e.qbdiag - 1) / e.qbdiag;
             err = launch_class(e.kdiag, grid_for(o, ntiles), e.smemdiag, d, c, ntiles, 0);
@@ -873,6 +901,7 @@ static int create_impl(const int32_t *atm, int natm, const int32_t *bas, int nba
     if (int e = own_alloc(o, &o->dm_cond, (size_t)nbas * nbas)) return bail(e);
     if (int e = own_alloc(o, &o->dm_max, 1)) return bail(e);
     if (int e = own_alloc(o, &o->counters, 4 * NQCLASS)) return bail(e);
+    if (int e = own_alloc(o, &o->qhist, 4 * NQCLASS)) return bail(e);
     if (int e = own_alloc(o, &o->work, 4 * NQCLASS)) return bail(e);
     *out = o;
     return 0;
@@ -911,6 +940,21 @@ static int ensure_workspace(jk_opt *o, int n_dm) {
     return 0;
 }
 
+static int ensure_fx(jk_opt *o, int n_dm) {
+    if (n_dm <= o->fx_ndm) return 0;
+    for (void *p : {(void *)o->jfx, (void *)o->kfx}) {
+        if (!p) continue;
+        auto it = std::find(o->owned.begin(), o->owned.end(), p);
+        if (it != o->owned.end()) o->owned.erase(it);
+        cudaFree(p);
+    }
+    size_t nn = (size_t)o->ntot;
+    if (int e = own_alloc(o, &o->jfx, nn * 2 * n_dm)) return e;
+    if (int e = own_alloc(o, &o->kfx, nn * 2 * 2 * n_dm)) return e;
+    o->fx_ndm = n_dm;
+    return 0;
+}
+
 // Operator passes of a build: lr * erf(|omega| r)/r + sr * erfc(|omega| r)/r
 // = sr * (1/r) + (lr - sr) * erf(|omega| r)/r, one pass per nonzero term.
 struct OpPass { double omega2, scale; };
@@ -943,6 +987,8 @@ static int build_impl(jk_opt *o, const double *dm, int n_dm, int hermi, int with
     if (precision != JK_PREC_FP64 && !(split_thresh > 0)) return fail(JK_ERR_ARG, "jk_build: split_thresh must be > 0");
     cudaStream_t st = (cudaStream_t)stream;
     if (int e = ensure_workspace(o, n_dm)) return e;
+    if (o->det)
+        if (int e = ensure_fx(o, n_dm)) return e;
     const int mixed = precision != JK_PREC_FP64;
     const size_t nn = (size_t)o->ntot;
     const Layout L = layout_of(o);
@@ -967,9 +1013,16 @@ static int build_impl(jk_opt *o, const double *dm, int n_dm, int hermi, int with
     CK(cudaGetLastError());
     if (with_j) CK(cudaMemsetAsync(o->jt, 0, sizeof(double) * nn * n_dm, st));
     if (with_k) CK(cudaMemsetAsync(o->kt, 0, sizeof(double) * nn * n_dmk, st));
+    if (o->det) {
+        CK(cudaMemsetAsync(o->jfx, 0, sizeof(unsigned long long) * 2 * nn * n_dm, st));
+        CK(cudaMemsetAsync(o->kfx, 0, sizeof(unsigned long long) * 2 * nn * n_dmk, st));
+    }
     CK(cudaMemsetAsync(o->work, 0, sizeof(int) * 4 * NQCLASS, st));
     const bool want_stats = stats != nullptr;
     if (want_stats) CK(cudaMemsetAsync(o->counters, 0, sizeof(unsigned long long) * 4 * NQCLASS, st));
+    unsigned long long *qnow = o->qhist + o->qhist_cur * 2 * NQCLASS;
+    const unsigned long long *qprev = o->qhist_valid ? o->qhist + (1 - o->qhist_cur) * 2 * NQCLASS : nullptr;
+    CK(cudaMemsetAsync(qnow, 0, sizeof(unsigned long long) * 2 * NQCLASS, st));
 
     EngineDev d = base_engine(o);
     d.dm_cond = o->dm_cond;
@@ -981,6 +1034,12 @@ static int build_impl(jk_opt *o, const double *dm, int n_dm, int hermi, int with
     d.log_cut = o->tol > 0 ? (float)std::log(o->tol) : -1e30f;
     d.log_split = mixed ? (float)std::log(split_thresh) : 0.f;
     d.fp32_asym = precision == JK_PREC_MIXED_FP32ROOTS;
+    d.qprev = qprev;
+    d.qnow = qnow;
+    d.vj_fx = o->det ? o->jfx : nullptr;
+    d.vk_fx = o->det ? o->kfx : nullptr;
+    o->qhist_cur ^= 1;
+    o->qhist_valid = true;
     o->ev_slot.clear();
     if (o->time_classes) {
         size_t need = 4 * o->plan_classes.size() * npass;
@@ -1016,6 +1075,7 @@ static int build_impl(jk_opt *o, const double *dm, int n_dm, int hermi, int with
             c.same = a == b;
             c.nbk = o->nbk[b];
             c.nx = o->npairs[a] * o->nbk[b];
+            c.li = e.li; c.lj = e.lj; c.lk = e.lk; c.ll = e.ll;
             long long upper = (long long)o->npairs[a] * ((o->npairs[b] + e.qb64 - 1) / e.qb64 + o->nbk[b]);
             if (!d.with_j && !d.with_k) break;
             cudaStream_t ls = concurrent ? o->side[nlaunched++ % jk_opt::NSIDE] : st;
@@ -1050,6 +1110,12 @@ static int build_impl(jk_opt *o, const double *dm, int n_dm, int hermi, int with
     }
     {
         int grid = (int)std::min<size_t>((nn * n_dm + 255) / 256, (size_t)o->sm_count * 8);
+        if (o->det) {
+            int g2 = (int)std::min<size_t>((nn * n_dmk + 255) / 256, (size_t)o->sm_count * 8);
+            if (with_j) fx_to_double_kernel<<<grid, 256, 0, st>>>(o->jfx, nn * n_dm, o->jt);
+            if (with_k) fx_to_double_kernel<<<g2, 256, 0, st>>>(o->kfx, nn * n_dmk, o->kt);
+            launches += 2;
+        }
         epilogue_kernel<<<grid, 256, 0, st>>>(o->jt, o->kt, n_dm, L, hermi, with_j, with_k, vj, vk);
         ++launches;
     }
@@ -1107,6 +1173,12 @@ int jk_opt_set_mol_ndm(jk_opt *o, const int32_t *ndm) {
         if (ndm[m] < 0) return fail(JK_ERR_ARG, "jk_opt_set_mol_ndm: negative count");
     CK(cudaMemcpy(o->mol_ndm, ndm, sizeof(int) * o->nmol, cudaMemcpyHostToDevice));
     o->use_mol_ndm = true;
+    return 0;
+}
+
+int jk_opt_set_deterministic(jk_opt *o, int enable) {
+    if (!o) return fail(JK_ERR_ARG, "jk_opt_set_deterministic: null optimizer");
+    o->det = enable != 0;
     return 0;
 }
 
@@ -1172,6 +1244,7 @@ int jk_opt_tune(jk_opt *o, const double *dm, int n_dm, int hermi, int precision,
         c.same = a == b;
         c.nbk = o->nbk[b];
         c.nx = o->npairs[a] * o->nbk[b];
+        c.li = e.li; c.lj = e.lj; c.lk = e.lk; c.ll = e.ll;
         const long long upper = (long long)o->npairs[a] * ((o->npairs[b] + 127) / 128 + o->nbk[b]);
         for (int prec = 0; prec <= mixed && !err; ++prec) {
             c.class_id = prec ? NQCLASS + q : q;
@@ -1347,6 +1420,7 @@ extern "C" int jk_build_noalloc(jk_opt *o, const double *dm, int n_dm, int nao, 
             c.same = a == bcls;
             c.nbk = o->nbk[bcls];
             c.nx = o->npairs[a] * o->nbk[bcls];
+            c.li = e.li; c.lj = e.lj; c.lk = e.lk; c.ll = e.ll;
             c.class_id = q;
             c.work = work + 2 * q;
             c.q_off = o->off64[q]; c.ket_begin = o->kb64[q]; c.ket_end = o->ke64[q];

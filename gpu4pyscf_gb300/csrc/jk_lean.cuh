@@ -143,10 +143,12 @@ struct LeanSmem {
 // lane by lane: the atomics resolve in L2 and cost the FP64 pipe nothing,
 // where summing lanes first would.  FP32 quartets sum lanes that hit the same
 // element in FP32 (warp aggregation) and convert once.  All 32 lanes call it.
+// (In deterministic mode the FP32 quartets add lane by lane as well: a sum
+// over the lanes would depend on which quartets share a warp.)
 template <typename Real>
-__device__ __forceinline__ void lean_add(double *addr, Real v, Real *buf, int lane) {
-    if constexpr (sizeof(Real) == 8) {
-        if (addr != nullptr) atomicAdd(addr, v);
+__device__ __forceinline__ void lean_add(const EngineDev &d, bool isk, double *addr, Real v, Real *buf, int lane) {
+    if (sizeof(Real) == 8 || d.vj_fx != nullptr) {
+        if (addr != nullptr) jk_add(d, isk, addr, (double)v);
     } else {
         warp_agg_add(addr, v, buf, lane);
     }
@@ -200,7 +202,7 @@ __device__ __forceinline__ void lean_digest(const EngineDev &d, const ClassDev &
                     for (int cc = 0; cc < NFK; ++cc)
 #pragma unroll
                         for (int dd = 0; dd < NFL; ++dd) s += LEAN_E(a, b, cc, dd) * dkl[cc * NFL + dd];
-                    lean_add(vd ? V + (size_t)(ai + a) * nao + aj + b : nullptr, fac * s, aggbuf, lane);
+                    lean_add(d, false, vd ? V + (size_t)(ai + a) * nao + aj + b : nullptr, fac * s, aggbuf, lane);
                 }
 #pragma unroll
             for (int cc = 0; cc < NFK; ++cc)
@@ -211,7 +213,7 @@ __device__ __forceinline__ void lean_digest(const EngineDev &d, const ClassDev &
                     for (int a = 0; a < NFI; ++a)
 #pragma unroll
                         for (int b = 0; b < NFJ; ++b) s += LEAN_E(a, b, cc, dd) * dij[a * NFJ + b];
-                    lean_add(vd ? V + (size_t)(ak + cc) * nao + al + dd : nullptr, fac * s, aggbuf, lane);
+                    lean_add(d, false, vd ? V + (size_t)(ak + cc) * nao + al + dd : nullptr, fac * s, aggbuf, lane);
                 }
         }
     }
@@ -245,7 +247,7 @@ __device__ __forceinline__ void lean_digest(const EngineDev &d, const ClassDev &
                     for (int b = 0; b < NFJ; ++b)
 #pragma unroll
                         for (int dd = 0; dd < NFL; ++dd) s += LEAN_E(a, b, cc, dd) * djl[b * NFL + dd];
-                    lean_add(vd ? V + (size_t)(ai + a) * nao + ak + cc : nullptr, fac * s, aggbuf, lane);
+                    lean_add(d, true, vd ? V + (size_t)(ai + a) * nao + ak + cc : nullptr, fac * s, aggbuf, lane);
                 }
 #pragma unroll
             for (int a = 0; a < NFI; ++a)
@@ -256,7 +258,7 @@ __device__ __forceinline__ void lean_digest(const EngineDev &d, const ClassDev &
                     for (int b = 0; b < NFJ; ++b)
 #pragma unroll
                         for (int cc = 0; cc < NFK; ++cc) s += LEAN_E(a, b, cc, dd) * djk[b * NFK + cc];
-                    lean_add(vd ? V + (size_t)(ai + a) * nao + al + dd : nullptr, fac * s, aggbuf, lane);
+                    lean_add(d, true, vd ? V + (size_t)(ai + a) * nao + al + dd : nullptr, fac * s, aggbuf, lane);
                 }
 #pragma unroll
             for (int b = 0; b < NFJ; ++b)
@@ -267,7 +269,7 @@ __device__ __forceinline__ void lean_digest(const EngineDev &d, const ClassDev &
                     for (int a = 0; a < NFI; ++a)
 #pragma unroll
                         for (int dd = 0; dd < NFL; ++dd) s += LEAN_E(a, b, cc, dd) * dil[a * NFL + dd];
-                    lean_add(vd ? V + (size_t)(aj + b) * nao + ak + cc : nullptr, fac * s, aggbuf, lane);
+                    lean_add(d, true, vd ? V + (size_t)(aj + b) * nao + ak + cc : nullptr, fac * s, aggbuf, lane);
                 }
 #pragma unroll
             for (int b = 0; b < NFJ; ++b)
@@ -278,7 +280,7 @@ __device__ __forceinline__ void lean_digest(const EngineDev &d, const ClassDev &
                     for (int a = 0; a < NFI; ++a)
 #pragma unroll
                         for (int cc = 0; cc < NFK; ++cc) s += LEAN_E(a, b, cc, dd) * dik[a * NFK + cc];
-                    lean_add(vd ? V + (size_t)(aj + b) * nao + al + dd : nullptr, fac * s, aggbuf, lane);
+                    lean_add(d, true, vd ? V + (size_t)(aj + b) * nao + al + dd : nullptr, fac * s, aggbuf, lane);
                 }
         }
     }
@@ -319,6 +321,12 @@ rys_lean_kernel(EngineDev d, ClassDev c, int unused)
     const int nunits = __ldg(c.q_off + c.nx);
     const int gwarp = (blockIdx.x * LEAN_THREADS + threadIdx.x) >> 5;
     if (gwarp > 0 && (long long)gwarp * JK_MIN_UNITS >= nunits) return;
+    // (an eighth of the grid always stays, in case this build has far more
+    // quartets than the last)
+    if (gwarp >= (int)(gridDim.x * (LEAN_THREADS / 32)) / 8 && d.qprev != nullptr) {
+        const unsigned long long prev = d.qprev[c.class_id];
+        if (prev > 0 && (unsigned long long)gwarp * 32 * JK_Q_PER_LANE >= prev) return;
+    }
     int kcur = 0, kend = 0, bcur = 0;
     bool exhausted = false;
     int nq = 0, nst = 0;
@@ -358,6 +366,7 @@ rys_lean_kernel(EngineDev d, ClassDev c, int unused)
             }
             const int take = min(nq, need);
             const int rank = __popc(empty & lt);
+            if (d.qnow != nullptr && lane == 0 && take > 0) atomicAdd(d.qnow + c.class_id, (unsigned long long)take);
             if (!has && rank < take) {
                 const int2 e = wq[rank];
                 qb = e.x;

@@ -26,6 +26,7 @@ struct ClassEntry {
     const void *k64_alt;
     const void *k32_alt;
     int smem64_alt, smem32_alt, threads_alt;
+    int generic;                // 1: the generic-l kernel (classes with a g shell)
 };
 
 // Defined in the instantiation translation units, one per bra pair class.
@@ -39,5 +40,7 @@ void register_bra_class_6(ClassEntry *tab);
 void register_bra_class_7(ClassEntry *tab);
 void register_bra_class_8(ClassEntry *tab);
 void register_bra_class_9(ClassEntry *tab);
+// classes with a g shell (jk_generic.cu)
+void register_generic(ClassEntry *tab);
 
 }  // namespace jk

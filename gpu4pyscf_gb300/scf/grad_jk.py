@@ -39,7 +39,7 @@ import torch
 from ..gto.sorted_basis import SortedBasis
 from ..lib import libjk
 
-LMAX_GRAD = 2  # raised copies must stay within the kernels' f
+LMAX_GRAD = 3  # raised copies must stay within the kernels' g
 
 
 def _comps(l):

@@ -267,9 +267,14 @@ class RHF:
         for cycle in range(self.max_cycle):
             fock = h1e + vhf
             err = X.T @ (fock @ dm @ s1e - s1e @ dm @ fock) @ X
+            # the reference's rule (gpu4pyscf/scf/hf.py:176-179, cycles
+            # counted from 0): damping before the DIIS start, DIIS from
+            # cycle diis_start_cycle on, so the Fock matrix of the initial
+            # guess (not idempotent, its commutator no measure of the
+            # error) never enters the DIIS subspace
             if cycle < self.damp_cycles and fock_prev is not None and self.damp > 0:
                 fock = (1 - self.damp) * fock + self.damp * fock_prev
-            elif cycle >= self.diis_start_cycle - 1:
+            elif cycle >= self.diis_start_cycle:
                 fock = diis.update(fock, err)
             fock_prev = fock
             if self.level_shift > 0 and (self.level_shift_cycles is None or cycle < self.level_shift_cycles):

@@ -27,7 +27,7 @@ import torch
 from ..gto.sorted_basis import SortedBasis
 from ..lib import libjk
 
-LMAX = 3  # highest angular momentum handled by the GPU kernels (f)
+LMAX = 4  # highest angular momentum handled by the GPU kernels (g)
 
 
 def _as_device(dm):
@@ -48,6 +48,9 @@ class _VHFOpt:
         self.sorted_mol = None
         self.precision = 'fp64'
         self.split_thresh = 1e-6
+        # bitwise-reproducible J/K (fixed-point accumulation), off by default
+        self.deterministic = False
+        self._det_set = False
         self._handle = None
         self._coeff = None
         self.last_stats = None
@@ -86,6 +89,7 @@ class _VHFOpt:
                                 ctypes.byref(h))
         libjk.check(err, 'jk_opt_create')
         self._handle = h
+        self._det_set = False
         self._coeff = torch.as_tensor(smol.coeff, device='cuda')
         return self
 
@@ -151,6 +155,10 @@ class _VHFOpt:
         st = libjk.JKStats() if stats else None
         stream = torch.cuda.current_stream().cuda_stream
         lib = libjk.load()
+        if bool(self.deterministic) != self._det_set:
+            libjk.check(lib.jk_opt_set_deterministic(self._handle, int(bool(self.deterministic))),
+                        'jk_opt_set_deterministic')
+            self._det_set = bool(self.deterministic)
         omega, lr, sr = (float(x) for x in op)
         out = (vj.data_ptr() if with_j else None, vk.data_ptr() if with_k else None)
         if omega == 0. and lr == 1. and sr == 1.:

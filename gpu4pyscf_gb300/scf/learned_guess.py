@@ -89,6 +89,21 @@ class GuessModel:
         self.mu = np.zeros(NFEAT)
         self.sd = np.ones(NFEAT)
 
+    def save(self, path):
+        st = self.net.state()
+        np.savez(path, nblock=self.nblock, sizes=np.asarray(st['sizes']), mu=self.mu, sd=self.sd,
+                 **{'W%d' % i: w for i, w in enumerate(st['W'])}, **{'b%d' % i: b for i, b in enumerate(st['b'])})
+
+    @classmethod
+    def load(cls, path):
+        z = np.load(path)
+        sizes = [int(x) for x in z['sizes']]
+        m = cls(int(z['nblock']), hidden=sizes[1])
+        m.net.load({'W': [z['W%d' % i] for i in range(len(sizes) - 1)],
+                    'b': [z['b%d' % i] for i in range(len(sizes) - 1)]})
+        m.mu, m.sd = z['mu'], z['sd']
+        return m
+
     def _x(self, feats):
         return torch.as_tensor(((feats - self.mu) / self.sd).astype(np.float32), device='cuda')
 
@@ -197,6 +212,31 @@ def generate(confsets, holdout, conv_tol=1e-8, log=None):
     return data
 
 
+def generate_batched(confsets, holdout, conv_tol=1e-8, chunk=64, log=None):
+    """As ``generate``, with the SCFs of up to ``chunk`` conformers of one
+    base molecule run together by ``BatchRHF`` (one batched J/K build per
+    cycle), each from the SAD guess."""
+    from .hf_batch import BatchRHF
+    data = []
+    cycles = []
+    t0 = time.perf_counter()
+    for b, confs in enumerate(confsets):
+        train = confs[:len(confs) - holdout]
+        for i in range(0, len(train), chunk):
+            part = train[i:i + chunk]
+            mf = BatchRHF(part, conv_tol=conv_tol)
+            mf.kernel()
+            if not all(mf.converged):
+                raise RuntimeError('an SCF of the training set did not converge')
+            for mol, dm in zip(part, mf.dms):
+                data.append((mol, dm.cpu().numpy()))
+            cycles.extend(mf.cycles)
+        if log:
+            log('base %d: %d conformers, %.1f s' % (b, len(train), time.perf_counter() - t0))
+    generate_batched.mean_cycles = float(np.mean(cycles)) if cycles else None
+    return data
+
+
 def build_arrays(data, nblock):
     Xs, Ts, Ms = [], [], []
     for mol, dm in data:
@@ -287,12 +327,57 @@ def evaluate(model, mols, conv_tol=1e-8, n_raw=None):
     return res
 
 
-def run(nbase=10, nconf=60, holdout=10, basis='syn-def2-svp', epochs=300, seed=0, out=None, lr=2e-3, n_raw=20):
+def evaluate_batched(model, mols, conv_tol=1e-8, chunk=64):
+    """``evaluate`` with the SCFs batched (``BatchRHF``): per held-out
+    molecule the cycles to conv_tol and the converged energy from SAD and
+    from the learned guess (projected to the nearest idempotent density),
+    and the RMS element errors of both guesses against the density converged
+    from SAD."""
+    from .hf_batch import BatchRHF
+    rows = []
+    for i in range(0, len(mols), chunk):
+        part = mols[i:i + chunk]
+        a = BatchRHF(part, conv_tol=conv_tol)
+        e_sad = a.kernel()
+        raws = [model.predict_density(m) for m in part]
+        guesses = [a.single[k].project_density(r) for k, r in enumerate(raws)]
+        b = BatchRHF(part, conv_tol=conv_tol)
+        e_ml = b.kernel(dm0s=guesses)
+        c = BatchRHF(part, conv_tol=conv_tol)
+        e_raw = c.kernel(dm0s=raws)
+        for k, mol in enumerate(part):
+            d_conv = a.dms[k]
+            sad = torch.as_tensor(guess.sad_density(mol), device='cuda')
+            rms = lambda d: float(torch.sqrt(torch.mean((torch.as_tensor(d, device='cuda') - d_conv) ** 2)).item())
+            rows.append({'natm': mol.natm, 'nao': mol.nao, 'cycles_sad': a.cycles[k],
+                         'cycles_learned': b.cycles[k], 'cycles_learned_raw': c.cycles[k],
+                         'e_sad': e_sad[k], 'e_learned': e_ml[k], 'e_learned_raw': e_raw[k],
+                         'converged': bool(a.converged[k] and b.converged[k] and c.converged[k]),
+                         'rms_sad': rms(sad), 'rms_learned': rms(guesses[k]), 'rms_learned_raw': rms(raws[k])})
+    cs = np.array([r['cycles_sad'] for r in rows])
+    cl = np.array([r['cycles_learned'] for r in rows])
+    cr = np.array([r['cycles_learned_raw'] for r in rows])
+    de = np.array([r['e_learned'] - r['e_sad'] for r in rows])
+    der = np.array([r['e_learned_raw'] - r['e_sad'] for r in rows])
+    return {'n': len(rows), 'mean_cycles_sad': float(cs.mean()), 'mean_cycles_learned': float(cl.mean()),
+            'mean_cycles_learned_raw': float(cr.mean()),
+            'cycle_reduction': float(1 - cl.mean() / cs.mean()),
+            'cycle_reduction_raw': float(1 - cr.mean() / cs.mean()),
+            'max_abs_dE': float(np.abs(de).max()), 'max_abs_dE_raw': float(np.abs(der).max()),
+            'n_dE_above_1e-7': int((np.abs(de) > 1e-7).sum()),
+            'all_converged': all(r['converged'] for r in rows),
+            'mean_rms_sad': float(np.mean([r['rms_sad'] for r in rows])),
+            'mean_rms_learned': float(np.mean([r['rms_learned'] for r in rows])),
+            'mean_rms_learned_raw': float(np.mean([r['rms_learned_raw'] for r in rows])), 'rows': rows}
+
+
+def run(nbase=10, nconf=60, holdout=10, basis='syn-def2-svp', epochs=300, seed=0, out=None, lr=2e-3, n_raw=20,
+        batched=False):
     log = lambda m: print(m, flush=True)
     t0 = time.perf_counter()
     confsets = make_conformers(nbase, nconf, basis, seed)
     nblock = max(b - a for cs in confsets for (a, b) in block_slices(cs[0]))
-    data = generate(confsets, holdout, log=log)
+    data = generate_batched(confsets, holdout, log=log) if batched else generate(confsets, holdout, log=log)
     t_gen = time.perf_counter() - t0
     t1 = time.perf_counter()
     model = train(data, nblock, epochs=epochs, lr=lr, seed=seed, log=log)
@@ -301,12 +386,13 @@ def run(nbase=10, nconf=60, holdout=10, basis='syn-def2-svp', epochs=300, seed=0
     t2 = time.perf_counter()
     # interleave the bases so that a prefix (n_raw) covers all of them
     held = [held[(i % nbase) * holdout + i // nbase] for i in range(len(held))]
-    res = evaluate(model, held, n_raw=n_raw)
+    res = evaluate_batched(model, held) if batched else evaluate(model, held, n_raw=n_raw)
     res.update({'workload': '%d base molecules (8-20 heavy atoms, C/N/O/H, H-saturated) x %d conformers '
                             '(sigma 0.05 A), %s; %d held out' % (nbase, nconf, basis, len(held)),
                 'train_conformers': len(data), 'train_pairs': int(sum(m.natm * (m.natm + 1) // 2 for m, _ in data)),
                 'final_train_loss': model.loss_history[-1], 'first_train_loss': model.loss_history[0],
-                'chained_cycles': generate.chained_cycles, 'epochs': epochs, 'lr': lr,
+                'training_scf_cycles': (generate_batched.mean_cycles if batched else generate.chained_cycles),
+                'epochs': epochs, 'lr': lr, 'batched_scf': batched,
                 'generate_s': t_gen, 'train_s': t_train, 'evaluate_s': time.perf_counter() - t2})
     if out:
         slim = dict(res)
@@ -327,6 +413,8 @@ if __name__ == '__main__':
     ap.add_argument('--n-raw', type=int, default=20)
     ap.add_argument('--basis', default='syn-def2-svp')
     ap.add_argument('--out', default=None)
+    ap.add_argument('--batched', action='store_true', help='run the SCFs batched (BatchRHF)')
     a = ap.parse_args()
-    res, _ = run(a.bases, a.conformers, a.holdout, a.basis, a.epochs, out=a.out, lr=a.lr, n_raw=a.n_raw)
+    res, _ = run(a.bases, a.conformers, a.holdout, a.basis, a.epochs, out=a.out, lr=a.lr, n_raw=a.n_raw,
+                 batched=a.batched)
     print(json.dumps({k: v for k, v in res.items() if k != 'rows'}))

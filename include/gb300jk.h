@@ -150,6 +150,17 @@ int jk_opt_tune(jk_opt *opt, const double *dm, int n_dm, int hermi, int precisio
 int jk_opt_set_variant(jk_opt *opt, int q, int prec, int alt, int grid_per_sm);
 int jk_opt_get_variant(const jk_opt *opt, int q, int prec, int *alt, int *grid_per_sm);
 
+/* Deterministic accumulation (no counterpart in the reference, whose FP64
+ * atomics make J/K depend on the order the GPU adds them in).  When enabled,
+ * later jk_build / jk_build_batch / jk_build_rsh calls of this optimizer add
+ * every contribution as two 64-bit fixed-point integers per element
+ * (multiples of 2^-24 and of 2^-56), whose sums do not depend on the order
+ * of the additions: J and K are bitwise reproducible from run to run, within
+ * 2^-57 per contribution of the default FP64 accumulation.  Costs an extra
+ * 16 bytes per J/K element of workspace and a few FP64 instructions per
+ * atomic.  jk_build_noalloc does not use it. */
+int jk_opt_set_deterministic(jk_opt *opt, int enable);
+
 const char *jk_last_error(void);
 
 /* One-electron integrals over the raw Cartesian functions of a sorted basis

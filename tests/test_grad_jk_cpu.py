@@ -56,7 +56,8 @@ def test_extended_basis_layout():
     assert (ext['down'][ext['ax'] == 0] == -1).all()
 
 
-def test_f_shells_rejected():
-    mol = gto.M(atom='O 0 0 0; H 0 0 1.8', basis='syn-def2-tzvp', unit='B')
+def test_g_shells_rejected():
+    # raised copies of g shells would need l = 5, beyond the kernels
+    mol = gto.M(atom='O 0 0 0; H 0 0 1.8', basis=('syn-def2-svp', [[4, [1., 1.]]]), unit='B')
     with pytest.raises(NotImplementedError):
         grad_jk.extended_basis(SortedBasis(mol))

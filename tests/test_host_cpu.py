@@ -64,9 +64,11 @@ def test_library_exports_header_symbols():
         assert hasattr(lib, n), n
 
 
-def test_lmax_above_f_rejected():
+def test_lmax_above_g_rejected():
+    # l = 5 (h): the reference sends it to PySCF's CPU code; this engine has
+    # no CPU path and refuses it
     from gpu4pyscf_gb300.scf import jk
-    mol = gto.M(atom='C 0 0 0; H 0 0 1', basis=('sto-3g', [[4, [1., 1.]]]))
+    mol = gto.M(atom='C 0 0 0; H 0 0 1', basis=('sto-3g', [[5, [1., 1.]]]))
     with pytest.raises(NotImplementedError):
         jk._VHFOpt(mol).build()
 

@@ -16,8 +16,13 @@ def test_learned_guess_small():
     held = [m for cs in confsets for m in cs[-2:]]
     res = lg.evaluate(model, held, n_raw=0)
     assert res['all_converged']
+    # unchanged converged energy
     assert res['max_abs_dE'] < 1e-7
-    assert res['mean_cycles_learned'] <= res['mean_cycles_sad'] + 1
+    # what the trained network gains over the method without it: a guess
+    # closer to the converged density than SAD on every held-out conformer
+    for r in res['rows']:
+        assert r['rms_learned'] < r['rms_sad'], r
+    assert res['mean_cycles_learned'] <= res['mean_cycles_sad']
     mf = hf.RHF(held[0])
     mf.init_guess = 'learned'
     mf.guess_model = model

@@ -126,3 +126,22 @@ def test_fp32_alternative_kernels_vs_fp64():
     for q in range(nq):
         opt.set_variant(q, 1, 0, 0)
     opt.precision = 'fp64'
+
+
+def test_c30_j_only_vs_oracle():
+    """J-only builds screen with the Coulomb blocks D_ij, D_kl alone (the
+    J engine's screening): fewer quartets than a J/K build, the same J."""
+    import bench
+    import torch
+    from gpu4pyscf_gb300.scf import jk
+    mol = _c30()
+    dm = bench.make_density(mol)
+    opt = jk._VHFOpt(mol, direct_scf_tol=1e-13).build()
+    dms = opt.apply_coeff_C_mat_CT(torch.as_tensor(dm, device='cuda')[None]).contiguous()
+    ref_j, _ = _oracle_sorted(opt, dms[0].cpu().numpy())
+    _, _ = opt._build(dms, 1, True, True, stats=True)
+    n_jk = opt.last_stats['quartets_fp64']
+    vj, _ = opt._build(dms, 1, True, False, stats=True)
+    n_j = opt.last_stats['quartets_fp64']
+    assert n_j < n_jk
+    assert abs(vj[0].cpu().numpy() - ref_j).max() <= FP64_TOL
