@@ -233,44 +233,53 @@ rys_class_kernel(EngineDev d, ClassDev c, int ntiles_static)
         // no busy slot after the refill: the work is exhausted
         if (__syncthreads_count(tid < QB && slots[tid].valid) == 0) break;
 
-        // ---- S1: roots, weights, scalars (one thread per slot) ----
-        for (int s = tid; s < QB; s += JK_THREADS) {
+        // ---- S1: roots, weights, scalars.  FP64: one thread per (slot,
+        // root), so the root evaluation of a step spreads over NR times as
+        // many warps (and SM sub-partitions) instead of leaving most of them
+        // waiting at the barrier; FP32: one thread per slot ----
+        if constexpr (sizeof(Real) == 8) {
+            for (int t = tid; t < QB * NR; t += JK_THREADS) {
+                const int s = t / NR, r = t % NR;
+                const SlotInfo &si = slots[s];
+                if (!si.valid) continue;
+                const int pb = si.pb_off + si.step / si.npk;
+                const int pk = si.pk_off + si.step % si.npk;
+                const d4 a1 = d.pp_a[pb], a2 = d.pp_a[pk];
+                const d4 b1 = d.pp_b[pb], b2 = d.pp_b[pk];
+                const double ip1 = d.pp_ip[pb], ip2 = d.pp_ip[pk];
+                const double p = a1.x, q = a2.x;
+                const double rs = rsqrt(p + q);
+                const double ipq = rs * rs;
+                const double PQx = a1.y - a2.y, PQy = a1.z - a2.z, PQz = a1.w - a2.w;
+                const double T = p * q * ipq * (PQx * PQx + PQy * PQy + PQz * PQz);
+                double ur, wr;
+                rys_root_one_rs<NR>(T, p * q * ipq, d.omega2, d.rys_coef, r, ur, wr);
+                // the coefficients the three axes share (computed here once
+                // instead of in each of the axis tasks of S2)
+                const double qpq = q * ipq, ppq = p * ipq;
+                Real *x = rw + (s * NR + r) * S::NRW;
+                x[0] = ur;
+                x[1] = wr * (b1.w * b2.w * rs * d.op_scale);
+                x[2] = ur * (0.5 * ipq);
+                x[3] = 0.5 * ip1 - ur * qpq * (0.5 * ip1);
+                x[4] = 0.5 * ip2 - ur * ppq * (0.5 * ip2);
+                x[5] = ur * qpq;
+                x[6] = ur * ppq;
+                if (r == 0) {
+                    Real *m = sc + s * NSC;
+                    m[5] = b1.x; m[6] = b1.y; m[7] = b1.z;
+                    m[8] = b2.x; m[9] = b2.y; m[10] = b2.z;
+                    m[11] = PQx; m[12] = PQy; m[13] = PQz;
+                }
+            }
+        } else for (int s = tid; s < QB; s += JK_THREADS) {
             const SlotInfo &si = slots[s];
             if (!si.valid) continue;
             int pb = si.pb_off + si.step / si.npk;
             int pk = si.pk_off + si.step % si.npk;
             Real *myrw = rw + s * NR * S::NRW;
             Real *m = sc + s * NSC;
-            if constexpr (sizeof(Real) == 8) {
-                d4 a1 = d.pp_a[pb], a2 = d.pp_a[pk];
-                d4 b1 = d.pp_b[pb], b2 = d.pp_b[pk];
-                double ip1 = d.pp_ip[pb], ip2 = d.pp_ip[pk];
-                double p = a1.x, q = a2.x;
-                double rs = rsqrt(p + q);
-                double ipq = rs * rs;
-                double PQx = a1.y - a2.y, PQy = a1.z - a2.z, PQz = a1.w - a2.w;
-                double T = p * q * ipq * (PQx * PQx + PQy * PQy + PQz * PQz);
-                double pref = b1.w * b2.w * rs * d.op_scale;
-                double u[NR], w[NR];
-                rys_roots_rs<NR>(T, p * q * ipq, d.omega2, d.rys_coef, u, w);
-                // per root: the coefficients the three axes share (computed
-                // here once instead of in each of the axis tasks of S2)
-                const double h2p = 0.5 * ip1, h2q = 0.5 * ip2, qpq = q * ipq, ppq = p * ipq, h2pq = 0.5 * ipq;
-#pragma unroll
-                for (int r = 0; r < NR; ++r) {
-                    Real *x = myrw + r * S::NRW;
-                    x[0] = (Real)u[r];
-                    x[1] = (Real)(w[r] * pref);
-                    x[2] = (Real)(u[r] * h2pq);
-                    x[3] = (Real)(h2p - u[r] * qpq * h2p);
-                    x[4] = (Real)(h2q - u[r] * ppq * h2q);
-                    x[5] = (Real)(u[r] * qpq);
-                    x[6] = (Real)(u[r] * ppq);
-                }
-                m[5] = (Real)b1.x; m[6] = (Real)b1.y; m[7] = (Real)b1.z;
-                m[8] = (Real)b2.x; m[9] = (Real)b2.y; m[10] = (Real)b2.z;
-                m[11] = (Real)PQx; m[12] = (Real)PQy; m[13] = (Real)PQz;
-            } else {
+            {
                 float4 a1 = d.pp_af[pb], a2 = d.pp_af[pk];
                 float4 b1 = d.pp_bf[pb], b2 = d.pp_bf[pk];
                 float ip1 = d.pp_ipf[pb], ip2 = d.pp_ipf[pk];

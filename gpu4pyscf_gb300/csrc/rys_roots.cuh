@@ -87,6 +87,51 @@ __device__ __forceinline__ void rys_roots(double T, const double *__restrict__ c
     for (int r = 0; r < NR; ++r) { u[r] = a[r]; w[r] = a[NR + r]; }
 }
 
+// One root r (u_r, w_r) of the FP64 quadrature: the same branch, interval
+// and Horner steps as rys_roots, for the two columns of root r only (a
+// block spreads the roots of a quartet over NR threads).
+template <int NR>
+__device__ __forceinline__ void rys_root_one(double T, int r, const double *__restrict__ coef, double &u, double &w) {
+    const int hi = __double2hiint(T);
+    if (hi >= dbl_hi_of_int(rys_tmax(NR))) {
+        const double rs = rsqrt(T);
+        constexpr int o = NR * (NR - 1) / 2;
+        u = c_rys_asym_x2[o + r] * rs * rs;
+        w = c_rys_asym_w[o + r] * rs;
+        return;
+    }
+    const int e = ((hi >> 20) & 0x7ff) - 1023;
+    const int m = (hi & 0xfffff) | 0x100000;
+    const int sh = 19 - e;
+    const int k = sh > 20 ? 0 : (m >> sh);
+    const int n = 2 * k + 1;
+    const int b = 31 - __clz(n);
+    const double centre = __hiloint2double(((1023 + b - 2) << 20) | ((n - (1 << b)) << (20 - b)), 0);
+    const double x = T - centre;
+    const double *c = coef + rys_off(NR) + k * (RYS_DEG + 1) * 2 * NR;
+    double a0 = __ldg(c + RYS_DEG * 2 * NR + r), a1 = __ldg(c + RYS_DEG * 2 * NR + NR + r);
+#pragma unroll
+    for (int i = RYS_DEG - 1; i >= 0; --i) {
+        a0 = fma(a0, x, __ldg(c + i * 2 * NR + r));
+        a1 = fma(a1, x, __ldg(c + i * 2 * NR + NR + r));
+    }
+    u = a0;
+    w = a1;
+}
+
+template <int NR>
+__device__ __forceinline__ void rys_root_one_rs(double T, double rho, double omega2, const double *__restrict__ coef,
+                                                int r, double &u, double &w) {
+    if (__double2hiint(omega2) <= 0) {
+        rys_root_one<NR>(T, r, coef, u, w);
+        return;
+    }
+    const double theta = omega2 / (omega2 + rho);
+    rys_root_one<NR>(T * theta, r, coef, u, w);
+    u *= theta;
+    w *= sqrt(theta);
+}
+
 // FP32 table staged in shared memory by a kernel: the block of NR roots,
 // one interval every rys_f_stride(NR) floats.  The stride is odd, so lanes
 // evaluating different intervals read different banks (every class has

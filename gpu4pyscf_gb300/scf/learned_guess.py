@@ -353,6 +353,8 @@ def evaluate_batched(model, mols, conv_tol=1e-8, chunk=64):
                          'cycles_learned': b.cycles[k], 'cycles_learned_raw': c.cycles[k],
                          'e_sad': e_sad[k], 'e_learned': e_ml[k], 'e_learned_raw': e_raw[k],
                          'converged': bool(a.converged[k] and b.converged[k] and c.converged[k]),
+                         'conv_sad': bool(a.converged[k]), 'conv_learned': bool(b.converged[k]),
+                         'conv_raw': bool(c.converged[k]),
                          'rms_sad': rms(sad), 'rms_learned': rms(guesses[k]), 'rms_learned_raw': rms(raws[k])})
     cs = np.array([r['cycles_sad'] for r in rows])
     cl = np.array([r['cycles_learned'] for r in rows])
@@ -366,6 +368,9 @@ def evaluate_batched(model, mols, conv_tol=1e-8, chunk=64):
             'max_abs_dE': float(np.abs(de).max()), 'max_abs_dE_raw': float(np.abs(der).max()),
             'n_dE_above_1e-7': int((np.abs(de) > 1e-7).sum()),
             'all_converged': all(r['converged'] for r in rows),
+            'converged_sad': int(sum(r['conv_sad'] for r in rows)),
+            'converged_learned': int(sum(r['conv_learned'] for r in rows)),
+            'converged_learned_raw': int(sum(r['conv_raw'] for r in rows)),
             'mean_rms_sad': float(np.mean([r['rms_sad'] for r in rows])),
             'mean_rms_learned': float(np.mean([r['rms_learned'] for r in rows])),
             'mean_rms_learned_raw': float(np.mean([r['rms_learned_raw'] for r in rows])), 'rows': rows}
