@@ -431,10 +431,13 @@ def run_scf(args):
     mol = make_mol(args.config)
     model, model_info = None, None
     arms = [('fp64', 'sad'), ('mixed', 'sad')]
-    if args.guess == 'learned':
+    if args.scf_arms:
+        arms = [tuple(a.split(':')) for a in args.scf_arms.split(',')]
+    if args.guess == 'learned' or any(g == 'learned' for _, g in arms):
         model, model_info = train_guess_model(CONFIGS[args.config]['basis'], args.guess_bases,
                                               args.guess_conformers, args.guess_epochs)
-        arms.append(('mixed', 'learned'))
+        if ('mixed', 'learned') not in arms:
+            arms.append(('mixed', 'learned'))
     rows = []
     for prec, g in arms:
         mf = hf.RHF(mol)
@@ -457,10 +460,70 @@ def run_scf(args):
             'higher_is_better': False, 'dtype': 'f64/mixed', 'data': 'synthetic',
             'config': {'workload': CONFIGS[args.config]['workload'], 'nao_user': mol.nao, 'natm': mol.natm,
                        'split': args.split},
-            'runs': rows, 'dE_vs_fp64_sad': [r['e_tot'] - rows[0]['e_tot'] for r in rows],
-            'speedup_vs_fp64_sad': [rows[0]['wall_s'] / r['wall_s'] for r in rows],
+            'runs': rows, 'dE_vs_first_run': [r['e_tot'] - rows[0]['e_tot'] for r in rows],
+            'speedup_vs_first_run': [rows[0]['wall_s'] / r['wall_s'] for r in rows],
             'guess_model': model_info}
     print(json.dumps(line))
+
+
+def run_profile(args):
+    """bench.py --mode profile: the J/K build of --config (FP64, or
+    --precision mixed with --split), per-class kernel times from CUDA events
+    (serialised), then one more build inside the NVTX range 'jk_profile', the
+    launch a profiler selects (ncu --nvtx --nvtx-include 'jk_profile/')."""
+    import torch
+    from gpu4pyscf_gb300.lib import libjk
+    from gpu4pyscf_gb300.scf import jk
+    mol = make_mol(args.config)
+    dm = make_density(mol)
+    opt = jk._VHFOpt(mol, direct_scf_tol=1e-13).build()
+    opt.precision, opt.split_thresh = args.precision, args.split
+    dms = opt.apply_coeff_C_mat_CT(torch.as_tensor(dm, device='cuda')[None]).contiguous()
+    lib = libjk.load()
+    opt._build(dms, 1, True, True, stats=True)
+    st = dict(opt.last_stats)
+    for _ in range(3):
+        opt._build(dms, 1, True, True)
+    ts = []
+    for _ in range(5):
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        opt._build(dms, 1, True, True)
+        e1.record()
+        torch.cuda.synchronize()
+        ts.append(e0.elapsed_time(e1))
+    h = opt._handle
+    lib.jk_opt_time_classes(h, 1)
+    opt._build(dms, 1, True, True, stats=True)
+    nq = lib.jk_n_quartet_classes()
+    ms = np.zeros(2 * nq)
+    fl = np.zeros(2 * nq, dtype=np.int64)
+    qq = np.zeros(2 * nq, dtype=np.int64)
+    L = [np.zeros(nq, dtype=np.int32) for _ in range(4)]
+    best = np.full(2 * nq, np.inf)
+    for _ in range(3):
+        opt._build(dms, 1, True, True)
+        lib.jk_opt_class_times(h, ms.ctypes.data, fl.ctypes.data, qq.ctypes.data, *[x.ctypes.data for x in L])
+        best = np.minimum(best, np.where(ms > 0, ms, np.inf))
+    lib.jk_opt_time_classes(h, 0)
+    rows = []
+    for k in range(2 * nq):
+        if np.isfinite(best[k]):
+            q = k // 2
+            rows.append(['(%d%d|%d%d) %s' % (L[0][q], L[1][q], L[2][q], L[3][q], 'FP32' if k % 2 else 'FP64'),
+                         round(float(best[k]), 4), int(qq[k]), int(fl[k]),
+                         round(fl[k] / (best[k] * 1e-3) / 1e12, 4)])
+    rows.sort(key=lambda r: -r[1])
+    torch.cuda.synchronize()
+    nvtx_push('jk_profile')
+    opt._build(dms, 1, True, True)
+    torch.cuda.synchronize()
+    nvtx_pop()
+    print(json.dumps({'mode': 'profile', 'config': CONFIGS[args.config]['workload'], 'precision': args.precision,
+                      'split': args.split if args.precision != 'fp64' else None, 'build_ms': sorted(ts),
+                      'stats': st, 'classes': {'columns': ['class', 'ms', 'quartets', 'model_flops', 'TFLOP/s'],
+                                               'rows': rows}}))
 
 
 def run_guess(args):
@@ -785,12 +848,17 @@ def main():
     ap.add_argument('--ref-seconds', type=float, default=20.)
     ap.add_argument('--no-cpu', action='store_true')
     ap.add_argument('--no-batch', action='store_true')
-    ap.add_argument('--mode', default='jk', choices=['jk', 'scf', 'dense', 'guess'],
+    ap.add_argument('--precision', default='fp64', choices=['fp64', 'mixed', 'mixed-fp32roots'],
+                    help='--mode profile: precision of the profiled build')
+    ap.add_argument('--mode', default='jk', choices=['jk', 'scf', 'dense', 'guess', 'profile'],
                     help='jk: the J/K benchmark line; scf: full RHF of --config (e.g. c120); '
                          'dense: FP64 vs mixed J/K of a dense SCF density of --config; '
-                         'guess: the learned initial guess against SAD')
+                         'guess: the learned initial guess against SAD; '
+                         'profile: per-class times and one build in the NVTX range jk_profile')
     ap.add_argument('--guess', default='sad', choices=['sad', 'learned'],
                     help='--mode scf: add a mixed-precision run from the learned guess')
+    ap.add_argument('--scf-arms', default=None,
+                    help='--mode scf: comma list of precision:guess runs (default fp64:sad,mixed:sad)')
     ap.add_argument('--guess-bases', type=int, default=40)
     ap.add_argument('--guess-conformers', type=int, default=50)
     ap.add_argument('--guess-holdout', type=int, default=5)
@@ -804,6 +872,8 @@ def main():
         run_dense(args)
     elif args.mode == 'guess':
         run_guess(args)
+    elif args.mode == 'profile':
+        run_profile(args)
     else:
         run_gpu(args)
 

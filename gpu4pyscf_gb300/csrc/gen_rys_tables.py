@@ -225,6 +225,10 @@ def main():
     lines.append('#define RYS_ASYM_SIZE %d' % len(hx))
     lines.append('#define RYS_ASYM_X2_LIST %s' % ', '.join(float.hex(v) for v in hx))
     lines.append('#define RYS_ASYM_W_LIST %s' % ', '.join(float.hex(v) for v in hw))
+    # FP32 copies for the FP32 asymptote (no conversion instruction, which
+    # would run on the FP64 pipe)
+    lines.append('#define RYS_ASYM_X2_LIST_F %s' % ', '.join('%.9ef' % v for v in hx))
+    lines.append('#define RYS_ASYM_W_LIST_F %s' % ', '.join('%.9ef' % v for v in hw))
     lines.append('static const double rys_asym_x2_host[RYS_ASYM_SIZE] = {RYS_ASYM_X2_LIST};')
     lines.append('static const double rys_asym_w_host[RYS_ASYM_SIZE] = {RYS_ASYM_W_LIST};')
     out = os.path.join(os.path.dirname(os.path.abspath(__file__)), 'rys_tables.inc')

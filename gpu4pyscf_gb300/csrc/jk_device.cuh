@@ -142,6 +142,19 @@ __device__ __forceinline__ bool pair_passes(const EngineDev &d, const ClassDev &
     return true;
 }
 
+// float -> double on the integer pipe: the exponent rebiased, the
+// significand shifted into place (normal numbers exactly; zero and FP32
+// denormals, below 1.2e-38, become 0).  GB300 runs the F2F conversion
+// instruction on its FP64 pipe, the scarce one, which the FP32 quartets
+// would otherwise spend on every contribution they add to J and K.
+__device__ __forceinline__ double widen_f32(float f) {
+    const unsigned u = __float_as_uint(f);
+    const unsigned ex = (u >> 23) & 0xffu;
+    const unsigned hi = (u & 0x80000000u) | ((ex + 896u) << 20) | ((u & 0x7fffffu) >> 3);
+    const unsigned lo = u << 29;
+    return ex == 0u ? 0. : __hiloint2double((int)hi, (int)lo);
+}
+
 // Adds v to J (isk false) or K element *addr.  Default: one FP64 atomic.
 // Deterministic mode: v = a 2^-24 + b 2^-56 (a = rint(v 2^24), b the
 // rounded remainder, |b| <= 2^31) goes into two 64-bit integer sums per

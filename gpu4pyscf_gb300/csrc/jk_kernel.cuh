@@ -118,7 +118,7 @@ rys_class_kernel(EngineDev d, ClassDev c, int ntiles_static)
     int chunk = blockIdx.x;
     const int nunits = MODE == MODE_JK ? __ldg(c.q_off + c.nx) : 0;
     if (MODE == MODE_JK && blockIdx.x > 0 && (long long)blockIdx.x * JK_MIN_UNITS >= nunits) return;
-    if (MODE == MODE_JK && blockIdx.x >= gridDim.x / 2 && d.qprev != nullptr) {
+    if (MODE == MODE_JK && sizeof(Real) == 8 && blockIdx.x >= gridDim.x / 2 && d.qprev != nullptr) {
         const unsigned long long prev = d.qprev[c.class_id];
         if (prev > 0 && (unsigned long long)blockIdx.x * QB * JK_Q_PER_LANE >= prev) return;
     }
@@ -508,7 +508,8 @@ rys_class_kernel(EngineDev d, ClassDev c, int ntiles_static)
                         out = V + (size_t)(aj + b) * nao + al + dd;
                     }
                 }
-                jk_add(d, isk, out, (double)si.fac * (double)sum);
+                if constexpr (sizeof(Real) == 4) jk_add(d, isk, out, widen_f32(si.fac * sum));
+                else jk_add(d, isk, out, (double)si.fac * (double)sum);
             }
         }
         if (my_fin) {

@@ -110,7 +110,10 @@ __device__ __forceinline__ void warp_agg_add(double *addr, Real v, Real *buf, in
             s += buf[__ffs(m) - 1];
             m &= m - 1;
         }
-        if (s != Real(0)) atomicAdd(addr, (double)s);
+        if (s != Real(0)) {
+            if constexpr (sizeof(Real) == 4) atomicAdd(addr, widen_f32(s));
+            else atomicAdd(addr, (double)s);
+        }
     }
     __syncwarp();
 }
@@ -148,7 +151,10 @@ struct LeanSmem {
 template <typename Real>
 __device__ __forceinline__ void lean_add(const EngineDev &d, bool isk, double *addr, Real v, Real *buf, int lane) {
     if (sizeof(Real) == 8 || d.vj_fx != nullptr) {
-        if (addr != nullptr) jk_add(d, isk, addr, (double)v);
+        if (addr != nullptr) {
+            if constexpr (sizeof(Real) == 4) jk_add(d, isk, addr, widen_f32(v));
+            else jk_add(d, isk, addr, (double)v);
+        }
     } else {
         warp_agg_add(addr, v, buf, lane);
     }
@@ -323,7 +329,9 @@ rys_lean_kernel(EngineDev d, ClassDev c, int unused)
     if (gwarp > 0 && (long long)gwarp * JK_MIN_UNITS >= nunits) return;
     // (an eighth of the grid always stays, in case this build has far more
     // quartets than the last)
-    if (gwarp >= (int)(gridDim.x * (LEAN_THREADS / 32)) / 8 && d.qprev != nullptr) {
+    // (FP32 launches keep their grid: their quartets are cheap and their
+    // time is latency, which more warps hide)
+    if (sizeof(Real) == 8 && gwarp >= (int)(gridDim.x * (LEAN_THREADS / 32)) / 8 && d.qprev != nullptr) {
         const unsigned long long prev = d.qprev[c.class_id];
         if (prev > 0 && (unsigned long long)gwarp * 32 * JK_Q_PER_LANE >= prev) return;
     }

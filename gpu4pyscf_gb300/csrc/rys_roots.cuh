@@ -14,6 +14,8 @@ namespace jk {
 
 __constant__ double c_rys_asym_x2[RYS_ASYM_SIZE] = {RYS_ASYM_X2_LIST};
 __constant__ double c_rys_asym_w[RYS_ASYM_SIZE] = {RYS_ASYM_W_LIST};
+__constant__ float c_rys_asym_x2_f[RYS_ASYM_SIZE] = {RYS_ASYM_X2_LIST_F};
+__constant__ float c_rys_asym_w_f[RYS_ASYM_SIZE] = {RYS_ASYM_W_LIST_F};
 
 static_assert(RYS_INV_WIDTH == 2, "the FP64 interval index below assumes intervals of width 1/2");
 
@@ -160,8 +162,8 @@ __device__ __forceinline__ void rys_roots_f(float T, const float *__restrict__ c
             constexpr int o = NR * (NR - 1) / 2;
 #pragma unroll
             for (int r = 0; r < NR; ++r) {
-                u[r] = (float)c_rys_asym_x2[o + r] * it;
-                w[r] = (float)c_rys_asym_w[o + r] * rs;
+                u[r] = c_rys_asym_x2_f[o + r] * it;
+                w[r] = c_rys_asym_w_f[o + r] * rs;
             }
             return;
         }
