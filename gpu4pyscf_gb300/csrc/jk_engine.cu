@@ -216,14 +216,21 @@ __global__ void plan_kernel(const PlanClass *pcs, int npc, int total, const floa
     }
     const int k = p.ket_mb0[mol] + kl;
     int b0 = p.ket_bstart[k], b1 = p.ket_bstart[k + 1];
+    // The kernels decide each quartet from the bound they compute
+    // themselves (pair_passes); these ranges only have to contain every
+    // quartet a kernel would take.  Float sums of logs associate differently
+    // here and there, so a bound at a threshold can round to opposite sides
+    // of it: every range is widened by PLAN_MARGIN in log space (a quartet
+    // dropped at the split would lose a contribution of the split's size).
+    constexpr float PLAN_MARGIN = 1e-3f;
     float base = p.bra_logq[ib] + dm_max[0];
-    int end = b0 + count_ge(p.ket_logq + b0, b1 - b0, log_cut - base);
+    int end = b0 + count_ge(p.ket_logq + b0, b1 - b0, log_cut - base - PLAN_MARGIN);
     int mid = end, beg32 = end;
     if (mixed) {
-        mid = min(end, b0 + count_ge(p.ket_logq + b0, b1 - b0, log_split - base));
+        mid = min(end, b0 + count_ge(p.ket_logq + b0, b1 - b0, log_split - base - PLAN_MARGIN));
         const int2 ij = p.bra_ij[ib];
         const float own = p.bra_logq[ib] + dm_cond[(size_t)ij.x * nbas + ij.y];
-        beg32 = min(end, b0 + count_ge(p.ket_logq + b0, b1 - b0, log_split - own));
+        beg32 = min(end, b0 + count_ge(p.ket_logq + b0, b1 - b0, log_split - own + PLAN_MARGIN));
     }
     if (p.same) {
         end = max(b0, min(end, ib + 1));

@@ -100,6 +100,33 @@ def test_batch_molecules_vs_oracle():
         assert abs(vk.cpu().numpy() - rk).max() <= FP64_TOL
 
 
+def test_batch_mixed_quartet_identity():
+    """The whole 64-molecule batch: every mixed build computes each screened
+    quartet exactly once (FP64 + FP32 counts equal the FP64 build's), so
+    its error against FP64 stays below the split's FP32 error and the
+    looser split never beats the tighter one by orders of magnitude."""
+    import bench
+    import torch
+    from gpu4pyscf_gb300.scf import jk_batch
+    mols, dms = bench.make_batch(nmol=64)
+    dd = [torch.as_tensor(d, device='cuda') for d in dms]
+    b = jk_batch.BatchJK([m for m, _ in mols])
+    j0, k0 = b.get_jk(dd, stats=True)
+    n64 = b.last_stats['quartets_fp64']
+    errs = {}
+    for split in (1e-8, 1e-6, 1e-4, 1e-6):
+        b.precision, b.split_thresh = 'mixed', split
+        jm, km = b.get_jk(dd, stats=True)
+        st = b.last_stats
+        assert st['quartets_fp64'] + st['quartets_fp32'] == n64, (split, st, n64)
+        err = max(max(float(abs(a - r).max()), float(abs(c - s).max()))
+                  for a, r, c, s in zip(jm, j0, km, k0))
+        assert err <= MIXED_TOL, (split, err)
+        errs[split] = err
+    assert errs[1e-6] < 10 * errs[1e-4] + 1e-12, errs
+    b.precision = 'fp64'
+
+
 def test_fp32_alternative_kernels_vs_fp64():
     """Every FP32 launch variant (the register-resident and the
     block-cooperative family, several grids) of a mixed build at a split
