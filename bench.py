@@ -402,7 +402,9 @@ def kernel_family(li, lj, lk, ll):
 # build, from one ncu capture of the c30 command (--set full, one launch of
 # the class inside the 'jk_timed' NVTX range); the roofline's traffic when
 # the dominant class is among them
-NCU_DRAM_BYTES = {('c30', '(21|11)'): 3100160, ('c30', '(11|10)'): 3365376}
+# DRAM read + write bytes of one launch of a class, from the full ncu captures
+# summarised in profiles/rys_fp64_kernels_c30.md (commands there)
+NCU_DRAM_BYTES = {('c30', '(11|11)'): 1685760 + 5376, ('c30', '(11|10)'): 3351808}
 
 
 def train_guess_model(basis, nbase, nconf, epochs, seed=0):
@@ -754,8 +756,9 @@ def run_gpu(args):
     traffic = NCU_DRAM_BYTES.get((args.config, dom['class']))
     roofline = {'bound': 'fp64', 'achieved': achieved, 'peak': peak64 / 1e12, 'unit': 'TFLOP/s',
                 'frac': achieved / (peak64 / 1e12), 'traffic': traffic,
-                'traffic_source': ('DRAM read + write of one launch of this class from the committed ncu '
-                                   'capture (profiles/), not measured in this run' if traffic else None),
+                'traffic_source': ('DRAM read + write of one launch of this class from the full ncu capture '
+                                   'in profiles/rys_fp64_kernels_c30.md (same code), not measured in this '
+                                   'run' if traffic else None),
                 'kernel': '%s %s FP64' % (kernel_family(*lk4), dom['class']), 'dominant': dom,
                 'peak_source': 'FP64 FMA-chain probe measured in this run (MEASURED_PEAKS.json has no FP64 figure)',
                 'fp32_peak_tflops': peak32 / 1e12,
