@@ -528,6 +528,52 @@ def run_profile(args):
                                                'rows': rows}}))
 
 
+def run_grad(args):
+    """bench.py --mode grad: nuclear gradient of the J/K energy of --config
+    (SAD density, j_factor 1, k_factor 0.5) through the dedicated derivative
+    kernels, timed with CUDA events (3 untimed, 5 timed), beside the route
+    through the J/K kernels of the extended basis (timed twice) and their
+    agreement; then one more gradient inside the NVTX range 'grad_profile'."""
+    import torch
+    from gpu4pyscf_gb300.scf import grad_jk, jk
+    mol = make_mol(args.config)
+    dm = make_density(mol)
+    opt = jk._VHFOpt(mol, direct_scf_tol=1e-13).build()
+    st = {}
+    g1 = grad_jk.jk_energy_grad(mol, dm, 1., .5, vhfopt=opt, stats=st)
+
+    def timed(fn, n):
+        ts = []
+        for _ in range(n):
+            torch.cuda.synchronize()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record()
+            fn()
+            e1.record()
+            torch.cuda.synchronize()
+            ts.append(e0.elapsed_time(e1) * 1e-3)
+        return sorted(ts)
+    for _ in range(3):
+        grad_jk.jk_energy_grad(mol, dm, 1., .5, vhfopt=opt)
+    t_ip1 = timed(lambda: grad_jk.jk_energy_grad(mol, dm, 1., .5, vhfopt=opt), 5)
+    g2 = grad_jk.jk_energy_grad(mol, dm, 1., .5, method='extended')
+    t_ext = timed(lambda: grad_jk.jk_energy_grad(mol, dm, 1., .5, method='extended'), 2)
+    torch.cuda.synchronize()
+    nvtx_push('grad_profile')
+    grad_jk.jk_energy_grad(mol, dm, 1., .5, vhfopt=opt)
+    torch.cuda.synchronize()
+    nvtx_pop()
+    d = (g1 - g2).abs().max().item()
+    print(json.dumps({'mode': 'grad', 'config': CONFIGS[args.config]['workload'], 'density': 'SAD',
+                      'j_factor': 1., 'k_factor': .5, 'natm': mol.natm,
+                      's_per_grad_ip1': t_ip1, 's_per_grad_extended': t_ext,
+                      'speedup_ip1_vs_extended': t_ext[0] / t_ip1[0], 'quartets': st.get('quartets'),
+                      'prim_quartets': st.get('prim_quartets'),
+                      'quartets_per_s': st.get('quartets', 0) / t_ip1[0],
+                      'max_abs_diff_ip1_vs_extended': d, 'max_abs_grad': g2.abs().max().item(),
+                      'translational_sum': g1.sum(0).abs().max().item()}))
+
+
 def run_guess(args):
     """bench.py --mode guess: the learned initial guess at the scale of the
     workload (seeded conformers of 8-20 heavy-atom C/N/O/H molecules,
@@ -853,11 +899,12 @@ def main():
     ap.add_argument('--no-batch', action='store_true')
     ap.add_argument('--precision', default='fp64', choices=['fp64', 'mixed', 'mixed-fp32roots'],
                     help='--mode profile: precision of the profiled build')
-    ap.add_argument('--mode', default='jk', choices=['jk', 'scf', 'dense', 'guess', 'profile'],
+    ap.add_argument('--mode', default='jk', choices=['jk', 'scf', 'dense', 'guess', 'profile', 'grad'],
                     help='jk: the J/K benchmark line; scf: full RHF of --config (e.g. c120); '
                          'dense: FP64 vs mixed J/K of a dense SCF density of --config; '
                          'guess: the learned initial guess against SAD; '
-                         'profile: per-class times and one build in the NVTX range jk_profile')
+                         'profile: per-class times and one build in the NVTX range jk_profile; '
+                         'grad: nuclear gradient of the J/K energy (derivative kernels)')
     ap.add_argument('--guess', default='sad', choices=['sad', 'learned'],
                     help='--mode scf: add a mixed-precision run from the learned guess')
     ap.add_argument('--scf-arms', default=None,
@@ -877,6 +924,8 @@ def main():
         run_guess(args)
     elif args.mode == 'profile':
         run_profile(args)
+    elif args.mode == 'grad':
+        run_grad(args)
     else:
         run_gpu(args)
 

@@ -67,7 +67,7 @@ def build(force=False, verbose=False, jobs=None):
         cmds.append([NVCC] + ARCH + FLAGS + ['-DJK_BRA_CLASS=%d' % b, '-c',
                                              os.path.join(HERE, 'jk_classes.cu'), '-o', o])
         objs.append(o)
-    for src in ('jk_engine.cu', 'jk_generic.cu', 'int1e.cu', 'mlp.cu'):
+    for src in ('jk_engine.cu', 'jk_generic.cu', 'jk_grad.cu', 'int1e.cu', 'mlp.cu'):
         o = os.path.join(BUILD, src.replace('.cu', '.o'))
         cmds.append([NVCC] + ARCH + FLAGS + ['-c', os.path.join(HERE, src), '-o', o])
         objs.append(o)

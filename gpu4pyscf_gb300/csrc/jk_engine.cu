@@ -163,6 +163,12 @@ __global__ void max_kernel(const float *x, int n, float *out) {
     if (threadIdx.x == 0) out[0] = red[0];
 }
 
+// Density part of the gradient screening bound over every quartet: twice
+// the largest log|D| block plus the larger of the J and K weight logs.
+__global__ void grad_bound_kernel(const float *dm_max, float log_j, float log_k, float *out) {
+    out[0] = 2.f * dm_max[0] + fmaxf(log_j, log_k);
+}
+
 struct PlanClass {
     const float *bra_logq;
     const float *ket_logq;
@@ -321,6 +327,11 @@ struct jk_opt {
     double *pp_ip = nullptr;
     float4 *pp_af = nullptr, *pp_bf = nullptr;
     float *pp_ipf = nullptr;
+    double2 *pp_e = nullptr;   // primitive exponents of every primitive pair (gradients)
+    int natm = 0;
+    int lmax = 0;              // highest shell angular momentum
+    int *shell_atom = nullptr;
+    float *grad_max = nullptr; // screening bound of a gradient build (device scalar)
     double *rys_coef = nullptr;
     float *rys_coef_f = nullptr;
     // sorted pair lists per pair class
@@ -441,6 +452,7 @@ int own_upload(jk_opt *o, T **p, const std::vector<T> &h) {
 struct PrimPairHost {
     std::vector<d4> a, b;
     std::vector<double> ip;
+    std::vector<double2> e;   // exponents (a, b) (gradient kernels)
 };
 
 // Primitive pairs of shell pair (i, j).  With prune, pairs whose Gaussian
@@ -484,6 +496,7 @@ int add_prim_pairs(const jk_opt *o, int i, int j, PrimPairHost &pp, bool prune =
             pp.a.push_back(d4{p, Px, Py, Pz});
             pp.b.push_back(d4{Px - A.x, Py - A.y, Pz - A.z, K});
             pp.ip.push_back(1.0 / p);
+            pp.e.push_back(make_double2(a, b));
             ++added;
         }
     return added;
@@ -656,13 +669,17 @@ static int create_impl(const int32_t *atm, int natm, const int32_t *bas, int nba
     CK(cudaGetDevice(&o->device));
     CK(cudaDeviceGetAttribute(&o->sm_count, cudaDevAttrMultiProcessorCount, o->device));
     if (int e = set_smem_attrs()) return bail(e);
+    if (int e = grad_set_smem_attrs())
+        return bail(fail(JK_ERR_CUDA, std::string("gradient kernels: ") + cudaGetErrorString((cudaError_t)e)));
     CK(cudaEventCreateWithFlags(&o->fork_ev, cudaEventDisableTiming));
     for (int i = 0; i < jk_opt::NSIDE; ++i) {
         CK(cudaStreamCreateWithFlags(&o->side[i], cudaStreamNonBlocking));
         CK(cudaEventCreateWithFlags(&o->join_ev[i], cudaEventDisableTiming));
     }
     o->nbas = nbas;
+    o->natm = natm;
     o->tol = tol;
+    std::vector<int> shell_atom_h;
     int ao = 0, prev_l = -1;
     for (int i = 0; i < nbas; ++i) {
         const int32_t *b = bas + 8 * i;
@@ -674,6 +691,8 @@ static int create_impl(const int32_t *atm, int natm, const int32_t *bas, int nba
             return bail(fail(JK_ERR_ARG, "shell primitive data out of range"));
         if (l < prev_l) return bail(fail(JK_ERR_ARG, "shells must be sorted by angular momentum"));
         prev_l = l;
+        o->lmax = std::max(o->lmax, l);
+        shell_atom_h.push_back(ia);
         int pcoord = atm[6 * ia + 1];
         if (pcoord < 0 || pcoord + 3 > nenv) return bail(fail(JK_ERR_ARG, "atom coordinate pointer out of range"));
         ShellDev s;
@@ -711,6 +730,7 @@ static int create_impl(const int32_t *atm, int natm, const int32_t *bas, int nba
     if (int e = own_upload(o, &o->mol_nao, o->mol_nao_h)) return bail(e);
     if (int e = own_alloc(o, &o->mol_ndm, (size_t)nmol)) return bail(e);
     if (int e = own_upload(o, &o->shells, o->shells_h)) return bail(e);
+    if (int e = own_upload(o, &o->shell_atom, shell_atom_h)) return bail(e);
     {
         std::vector<double> t(rys_coef_host, rys_coef_host + RYS_TABLE_SIZE);
         std::vector<float> tf(rys_coef_f_host, rys_coef_f_host + RYS_TABLE_F_SIZE);
@@ -861,6 +881,7 @@ static int create_impl(const int32_t *atm, int natm, const int32_t *bas, int nba
         if (int e = own_upload(o, &o->pp_af, af)) return bail(e);
         if (int e = own_upload(o, &o->pp_bf, bf)) return bail(e);
         if (int e = own_upload(o, &o->pp_ipf, ipf)) return bail(e);
+        if (int e = own_upload(o, &o->pp_e, fpp.e)) return bail(e);
     }
     // planning buffers
     std::vector<PlanClass> plan;
@@ -907,6 +928,7 @@ static int create_impl(const int32_t *atm, int natm, const int32_t *bas, int nba
     if (int e = own_upload(o, &o->scan_dev, scans)) return bail(e);
     if (int e = own_alloc(o, &o->dm_cond, (size_t)nbas * nbas)) return bail(e);
     if (int e = own_alloc(o, &o->dm_max, 1)) return bail(e);
+    if (int e = own_alloc(o, &o->grad_max, 1)) return bail(e);
     if (int e = own_alloc(o, &o->counters, 4 * NQCLASS)) return bail(e);
     if (int e = own_alloc(o, &o->qhist, 4 * NQCLASS)) return bail(e);
     if (int e = own_alloc(o, &o->work, 4 * NQCLASS)) return bail(e);
@@ -1172,6 +1194,126 @@ int jk_build_rsh(jk_opt *o, const double *dm, int n_dm, int nao, int hermi, int 
 }
 
 long long jk_opt_ntot(const jk_opt *o) { return o ? o->ntot : -1; }
+
+// Nuclear gradient of the J/K energy through the dedicated derivative
+// kernels (jk_grad.cu), with the optimizer's pair lists and its plan of
+// work units.  The plan runs with the gradient's bound (products of two
+// density blocks) in place of the J/K build's; the class kernels add their
+// per-atom sums into ejk on the side streams.
+int jk_energy_grad(jk_opt *o, const double *dm, int n_dm, int nao, double j_factor, double k_factor,
+                   double omega, double lr_factor, double sr_factor, double *ejk, void *stream,
+                   jk_stats *stats) {
+    if (!o || !dm || !ejk || n_dm < 1 || n_dm > 2 || o->nmol != 1 || nao != o->nao)
+        return fail(JK_ERR_ARG, "jk_energy_grad: invalid arguments");
+    if (!std::isfinite(j_factor) || !std::isfinite(k_factor))
+        return fail(JK_ERR_ARG, "jk_energy_grad: non-finite factors");
+    if (o->lmax > GRAD_LMAX)
+        return fail(JK_ERR_LMAX, "jk_energy_grad: shells above f are not supported by the gradient kernels");
+    OpPass passes[2];
+    const int npass = op_passes(omega, lr_factor, sr_factor, passes);
+    if (npass < 0 || !std::isfinite(omega) || !std::isfinite(lr_factor) || !std::isfinite(sr_factor))
+        return fail(JK_ERR_ARG, "jk_energy_grad: omega = 0 needs lr_factor == sr_factor");
+    cudaStream_t st = (cudaStream_t)stream;
+    CK(cudaMemsetAsync(ejk, 0, sizeof(double) * 3 * o->natm, st));
+    if (npass == 0 || (j_factor == 0. && k_factor == 0.)) return 0;
+    // weights of the density products (the reference's convention): 8-fold
+    // permutation symmetry and the 1/2 of the Coulomb energy give 4 j_factor;
+    // K takes (D_jk D_li + D_jl D_ki), and an RHF density (one matrix)
+    // carries both spins, which halves k_factor
+    const double jfac = 4. * j_factor;
+    const double kfac = -2. * (n_dm == 1 ? .5 : 1.) * k_factor;
+    const float log_j = jfac != 0. ? (float)(std::log(std::fabs(jfac)) + 2. * std::log((double)n_dm)) : -1e30f;
+    const float log_k = kfac != 0. ? (float)(std::log(2. * std::fabs(kfac) * n_dm)) : -1e30f;
+    const Layout L = layout_of(o);
+    const int nb2 = o->nbas * o->nbas;
+    dm_cond_kernel<<<(nb2 + 255) / 256, 256, 0, st>>>(dm, n_dm, L, o->shells, o->nbas, 1, o->dm_cond);
+    max_kernel<<<1, 1024, 0, st>>>(o->dm_cond, nb2, o->dm_max);
+    grad_bound_kernel<<<1, 1, 0, st>>>(o->dm_max, log_j, log_k, o->grad_max);
+    const float log_cut = o->tol > 0 ? (float)std::log(o->tol) : -1e30f;
+    if (o->nplan > 0) {
+        plan_kernel<<<(o->plan_total + 255) / 256, 256, 0, st>>>(o->plan_dev, o->nplan, o->plan_total, o->grad_max,
+                                                                 o->dm_cond, o->nbas, log_cut, 0.f, 0);
+        scan_kernel<<<o->nscan, 1024, 0, st>>>(o->scan_dev);
+    }
+    CK(cudaGetLastError());
+    CK(cudaMemsetAsync(o->work, 0, sizeof(int) * 4 * NQCLASS, st));
+    if (stats) CK(cudaMemsetAsync(o->counters, 0, sizeof(unsigned long long) * 4 * NQCLASS, st));
+    EngineDev d = base_engine(o);
+    d.dm_cond = o->dm_cond;
+    d.log_cut = log_cut;
+    d.counters = stats ? o->counters : nullptr;
+    GradDev g;
+    std::memset(&g, 0, sizeof(g));
+    g.pp_e = o->pp_e;
+    g.shell_atom = o->shell_atom;
+    g.dm = dm;
+    g.n_dm = n_dm;
+    g.nao = nao;
+    g.jfac = jfac;
+    g.kfac = kfac;
+    g.log_j = log_j;
+    g.log_k = log_k;
+    g.grad = ejk;
+    CK(cudaEventRecord(o->fork_ev, st));
+    for (int i = 0; i < jk_opt::NSIDE; ++i) CK(cudaStreamWaitEvent(o->side[i], o->fork_ev, 0));
+    int nlaunched = 0;
+    for (int ip = 0; ip < npass; ++ip) {
+        d.omega2 = passes[ip].omega2;
+        d.op_scale = passes[ip].scale;
+        int *work = o->work + ip * 2 * NQCLASS;
+        for (auto it = o->plan_classes.rbegin(); it != o->plan_classes.rend(); ++it) {
+            const int q = *it;
+            const ClassEntry &e = g_tab[q];
+            int a = 0;
+            while ((a + 1) * (a + 2) / 2 <= q) ++a;
+            const int b = q - a * (a + 1) / 2;
+            GradClass gc;
+            if (grad_class(e.li, e.lj, e.lk, e.ll, &gc))
+                return fail(JK_ERR_LMAX, "jk_energy_grad: class above the gradient kernels");
+            ClassDev c;
+            std::memset(&c, 0, sizeof(c));
+            c.bra = PairList{o->npairs[a], o->pl_ij[a], o->pl_logq[a], o->pl_prim[a], o->pl_cnt[a]};
+            c.ket = PairList{o->npairs[b], o->pl_ij[b], o->pl_logq[b], o->pl_prim[b], o->pl_cnt[b]};
+            c.same = a == b;
+            c.nbk = o->nbk[b];
+            c.nx = o->npairs[a] * o->nbk[b];
+            c.li = e.li; c.lj = e.lj; c.lk = e.lk; c.ll = e.ll;
+            c.class_id = q;
+            c.work = work + 2 * q;
+            c.q_off = o->off64[q]; c.ket_begin = o->kb64[q]; c.ket_end = o->ke64[q];
+            c.split_mode = SPLIT_ALL;
+            g.qb = gc.qb;
+            // one block per work unit at most; resident blocks of every SM
+            const long long upper = (long long)o->npairs[a] * ((o->npairs[b] + JK_KCHUNK - 1) / JK_KCHUNK + o->nbk[b]);
+            int per_sm = 0;
+            CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, gc.kernel, JK_THREADS, (size_t)gc.smem));
+            const int grid = (int)std::max<long long>(1, std::min<long long>(upper, (long long)o->sm_count * std::max(per_sm, 1)));
+            cudaStream_t ls = o->side[nlaunched++ % jk_opt::NSIDE];
+            void *args[] = {(void *)&d, (void *)&c, (void *)&g};
+            CK(cudaLaunchKernel(gc.kernel, dim3(grid), dim3(JK_THREADS), args, (size_t)gc.smem, ls));
+        }
+    }
+    for (int i = 0; i < jk_opt::NSIDE; ++i) {
+        CK(cudaEventRecord(o->join_ev[i], o->side[i]));
+        CK(cudaStreamWaitEvent(st, o->join_ev[i], 0));
+    }
+    CK(cudaGetLastError());
+    if (stats) {
+        std::memset(stats, 0, sizeof(*stats));
+        std::vector<unsigned long long> cnt(4 * NQCLASS);
+        CK(cudaStreamSynchronize(st));
+        CK(cudaMemcpy(cnt.data(), o->counters, sizeof(unsigned long long) * cnt.size(), cudaMemcpyDeviceToHost));
+        for (int q = 0; q < NQCLASS; ++q) {
+            stats->quartets_fp64 += (int64_t)cnt[2 * q];
+            stats->prim_quartets_fp64 += (int64_t)cnt[2 * q + 1];
+        }
+        stats->kernel_launches = 4 + 2 + npass * (int)o->plan_classes.size();
+        stats->n_classes = (int)o->plan_classes.size();
+    }
+    return 0;
+}
+
+int jk_opt_natm(const jk_opt *opt) { return opt ? opt->natm : -1; }
 
 int jk_opt_set_mol_ndm(jk_opt *o, const int32_t *ndm) {
     if (!o) return fail(JK_ERR_ARG, "jk_opt_set_mol_ndm: null optimizer");

@@ -43,4 +43,33 @@ void register_bra_class_9(ClassEntry *tab);
 // classes with a g shell (jk_generic.cu)
 void register_generic(ClassEntry *tab);
 
+// ---- nuclear-gradient kernels (jk_grad.cu)
+
+// highest angular momentum of the gradient kernels (the raised 2D integrals
+// reach GRAD_LMAX + 1)
+#define GRAD_LMAX 3
+
+struct GradDev {
+    const double2 *pp_e;      // exponents (a_i, a_j) of every primitive pair
+    const int *shell_atom;    // atom of every shell
+    const double *dm;         // [n_dm][nao][nao] densities in the sorted Cartesian basis
+    int n_dm, nao;
+    int qb;                   // quartets (slots) per block of the launch
+    double jfac, kfac;        // weights of the J and K density products
+    float log_j, log_k;       // their logs plus the density-count factors (screening)
+    double *grad;             // [natm][3] accumulators
+};
+
+struct GradClass {
+    const void *kernel;
+    int qb;      // slots per block
+    int smem;    // dynamic shared memory of a block
+};
+
+// Kernel, slots and shared memory of class (li lj|lk ll); nonzero when a
+// shell is above GRAD_LMAX.
+int grad_class(int li, int lj, int lk, int ll, GradClass *out);
+// Dynamic shared memory limits of the gradient kernels (cudaError_t code).
+int grad_set_smem_attrs();
+
 }  // namespace jk

@@ -1,22 +1,30 @@
-"""Nuclear gradient of the J/K energy, through the J/K engine.
+"""Nuclear gradient of the J/K energy.
 
 Counterpart of gpu4pyscf's ``_jk_energy_per_atom`` (gpu4pyscf/grad/rhf.py:
 60-171, kernel ``RYS_per_atom_jk_ip1`` in gpu4pyscf/lib/gvhf-rys/
-rys_contract_jk_ip1.cu:1747-1797) for an RHF density: the [natm, 3] gradient
-of
+rys_contract_jk_ip1.cu:1747-1797): the [natm, 3] gradient of
 
     E = j_factor/2 sum (ij|kl) D_ji D_lk - k_factor/4 sum (ij|kl) D_jk D_li
 
-with respect to the nuclear positions, at fixed (symmetric) D.
+with respect to the nuclear positions, at fixed densities.
 
-Method.  The derivative of a raw Cartesian primitive c x^a exp(-alpha r^2)
-along x is a_x times the function lowered by one in x minus the function
-raised by one with coefficient 2 alpha c.  So the derivative integrals are
-ordinary integrals over an extended basis holding, for every shell of the
-sorted basis, the shell itself, a copy with l + 1 and coefficients
-2 alpha c, and (l > 0) a copy with l - 1.  One J/K build of the extended
-basis, with the density on the original shells only, gives for every
-derived function i'
+Two routes.  The product path (``method='ip1'``) is the engine's dedicated
+derivative kernels (``jk_energy_grad`` of the C ABI, csrc/jk_grad.cu): per
+screened shell quartet the derivative integrals on three centres,
+contracted with the quartet's density weights into per-atom sums, with the
+optimizer's pair lists and work units; shells up to f.  It takes one
+(symmetric or antisymmetric) density, or two spin densities, as the
+reference does.
+
+The second route (``method='extended'``), kept as an independent check on
+the GPU, uses the J/K kernels unchanged.  The derivative of a raw Cartesian
+primitive c x^a exp(-alpha r^2) along x is a_x times the function lowered
+by one in x minus the function raised by one with coefficient 2 alpha c.
+So the derivative integrals are ordinary integrals over an extended basis
+holding, for every shell of the sorted basis, the shell itself, a copy
+with l + 1 and coefficients 2 alpha c, and (l > 0) a copy with l - 1.  One
+J/K build of the extended basis, with the density on the original shells
+only, gives for every derived function i'
 
     vj[i', j] = sum_kl (i'j|kl) D_lk,     vk[i', l] = sum_jk (i'j|kl) D_jk,
 
@@ -25,10 +33,8 @@ and with D symmetric the four centres of a quartet contribute alike:
     dE/dR_A = -4 sum_{i on A} [ j/2 sum_j (d_x i)vj[., j] D_ji
                                 - k/4 sum_l (d_x i)vk[., l] D_li ].
 
-The build runs the engine's J/K kernels unchanged (density screening drops
-the quartets the zero blocks cannot reach).  Raised copies of f shells
-would be g shells, which the kernels do not cover: bases with f shells
-raise NotImplementedError.
+Raised copies of f shells are g shells, the highest the J/K kernels take,
+so both routes stop at f.
 """
 
 import ctypes
@@ -133,12 +139,55 @@ def contract(ext, vj, vk, dm, natm, j_factor=1., k_factor=1.):
     return g
 
 
-def jk_energy_grad(mol, dm, j_factor=1., k_factor=1., direct_scf_tol=1e-13):
+def jk_energy_grad(mol, dm, j_factor=1., k_factor=1., direct_scf_tol=1e-13, method='ip1', vhfopt=None,
+                   stats=None):
     """[natm, 3] nuclear gradient (torch, cuda) of the J/K energy of the
-    symmetric user-basis density dm (gpu4pyscf/grad/rhf.py:60-171), with
-    the operator of mol.omega (libcint's sign convention)."""
+    user-basis density dm (gpu4pyscf/grad/rhf.py:60-171), with the operator
+    of mol.omega (libcint's sign convention).  dm: [nao, nao] (symmetric or
+    antisymmetric) or [2, nao, nao] spin densities (ip1 only).  vhfopt: a
+    built _VHFOpt of mol to reuse (ip1).  stats: a dict that receives the
+    quartet counts of the build (ip1; synchronises)."""
     from .jk import _env_operator
     omega, lr, sr = _env_operator(getattr(mol, 'omega', 0.) or 0.)
+    if method == 'ip1':
+        return _grad_ip1(mol, dm, j_factor, k_factor, direct_scf_tol, (omega, lr, sr), vhfopt, stats)
+    if method != 'extended':
+        raise ValueError('method must be ip1 or extended')
+    return _grad_extended(mol, dm, j_factor, k_factor, direct_scf_tol, (omega, lr, sr))
+
+
+def _grad_ip1(mol, dm, j_factor, k_factor, direct_scf_tol, op, vhfopt=None, stats=None):
+    from .jk import _VHFOpt
+    opt = vhfopt if vhfopt is not None else _VHFOpt(mol, direct_scf_tol=direct_scf_tol).build()
+    if opt._handle is None:
+        opt.build()
+    if opt.sorted_mol.lmax > LMAX_GRAD:
+        raise NotImplementedError('J/K gradients are supported for shells up to f')
+    d = torch.as_tensor(np.asarray(dm) if not isinstance(dm, torch.Tensor) else dm,
+                        dtype=torch.float64, device='cuda')
+    if d.ndim == 2:
+        d = d[None]
+    if d.ndim != 3 or d.shape[0] > 2:
+        raise ValueError('dm must be [nao, nao] or [2, nao, nao]')
+    ds = opt.apply_coeff_C_mat_CT(d).contiguous()
+    lib = libjk.load()
+    natm = lib.jk_opt_natm(opt._handle)
+    ejk = torch.empty((natm, 3), dtype=torch.float64, device='cuda')
+    omega, lr, sr = op
+    st = libjk.JKStats() if stats is not None else None
+    libjk.check(lib.jk_energy_grad(opt._handle, ds.data_ptr(), int(ds.shape[0]), int(ds.shape[-1]),
+                                   float(j_factor), float(k_factor), float(omega), float(lr), float(sr),
+                                   ejk.data_ptr(), torch.cuda.current_stream().cuda_stream,
+                                   ctypes.byref(st) if st is not None else None), 'jk_energy_grad')
+    if st is not None:
+        d = st.as_dict()
+        stats.update(quartets=d['quartets_fp64'], prim_quartets=d['prim_quartets_fp64'],
+                     kernel_launches=d['kernel_launches'])
+    return ejk
+
+
+def _grad_extended(mol, dm, j_factor, k_factor, direct_scf_tol, op):
+    omega, lr, sr = op
     sb = SortedBasis(mol)
     ext = extended_basis(sb)
     lib = libjk.load()
@@ -174,11 +223,12 @@ def jk_energy_grad(mol, dm, j_factor=1., k_factor=1., direct_scf_tol=1e-13):
 def _jk_energy_per_atom(vhfopt, dm, j_factor=1., k_factor=1., omega=None, lr_factor=None,
                         sr_factor=None, verbose=None):
     """The reference's entry (gpu4pyscf/grad/rhf.py:60): [natm, 3] numpy
-    gradient of j_factor * E_J - k_factor * E_K for the RHF density dm, with
-    the optimizer's molecule and screening threshold.  As in the reference,
-    explicit range-separation factors are not accepted; mol.omega applies."""
+    gradient of j_factor * E_J - k_factor * E_K for dm ([nao, nao] or two
+    spin densities), with the optimizer's molecule, screening threshold and
+    pair lists.  As in the reference, explicit range-separation factors are
+    not accepted; mol.omega applies."""
     assert lr_factor is None and sr_factor is None
     mol = vhfopt.mol
     if omega is not None and omega != (getattr(mol, 'omega', 0.) or 0.):
         raise NotImplementedError('omega other than mol.omega')
-    return jk_energy_grad(mol, dm, j_factor, k_factor, vhfopt.direct_scf_tol).cpu().numpy()
+    return jk_energy_grad(mol, dm, j_factor, k_factor, vhfopt.direct_scf_tol, vhfopt=vhfopt).cpu().numpy()

@@ -92,6 +92,9 @@ long long jk_opt_ntot(const jk_opt *opt);
 /* Number of Cartesian AOs of the sorted basis. */
 int jk_opt_nao(const jk_opt *opt);
 
+/* Number of atoms of the basis the optimizer was created with. */
+int jk_opt_natm(const jk_opt *opt);
+
 /* Number of significant shell pairs kept after Schwarz screening. */
 int jk_opt_npairs(const jk_opt *opt);
 
@@ -135,6 +138,29 @@ int jk_build_rsh(jk_opt *opt, const double *dm, int n_dm, int nao, int hermi,
                  int with_j, int with_k, double omega, double lr_factor, double sr_factor,
                  int precision, double split_thresh, double *vj, double *vk,
                  void *stream, jk_stats *stats);
+
+/* Nuclear gradient of the J/K energy; replaces RYS_per_atom_jk_ip1
+ * (gpu4pyscf/lib/gvhf-rys/rys_contract_jk_ip1.cu:1747-1797) as called by
+ * _jk_energy_per_atom (gpu4pyscf/grad/rhf.py:60-171).
+ * ejk[A][x] = dE/dR_A,x of
+ *     E = j_factor/2 sum (ij|kl) D_ji D_lk - k_factor/4 sum (ij|kl) D_jk D_li
+ * at fixed densities, for a symmetric or antisymmetric density (n_dm = 1,
+ * an RHF density; the K weight uses D_jk D_li + D_jl D_ki) or a pair of
+ * spin densities (n_dm = 2: J of their sum, K of each, k_factor not
+ * halved), the reference's weights for both.
+ * dm: device [n_dm][nao][nao] float64 in the sorted Cartesian basis of a
+ *     single-molecule optimizer.
+ * omega, lr_factor, sr_factor: the operator as in jk_build_rsh (0, 1, 1 for
+ *     the Coulomb operator).
+ * ejk: device [jk_opt_natm()][3] float64 output, overwritten.
+ * Screening: q_ij q_kl times the largest density product of the quartet's
+ * weight against the optimizer's tolerance.  Shells up to f
+ * (JK_ERR_LMAX above).  Asynchronous on stream unless stats (optional host
+ * output: quartets and primitive quartets evaluated, in the FP64 fields) is
+ * given, which synchronises. */
+int jk_energy_grad(jk_opt *opt, const double *dm, int n_dm, int nao, double j_factor,
+                   double k_factor, double omega, double lr_factor, double sr_factor,
+                   double *ejk, void *stream, jk_stats *stats);
 
 /* Autotuner (no counterpart in the reference, whose launch schemes are
  * fixed per class).  jk_opt_tune times, for every angular class (and
