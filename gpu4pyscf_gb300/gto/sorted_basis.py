@@ -4,7 +4,13 @@ The restatement of what gpu4pyscf's SortedGTO.from_mol prepares
 (gpu4pyscf/gto/mole.py:585-654): general contractions are split into one
 shell per contraction, shells are sorted by angular momentum (then by
 primitive count, descending) and all integrals are evaluated over raw
-Cartesian functions.  The map between the user basis (spherical or
+Cartesian functions.  With diffuse_cutoff > 0 every primitive with an
+exponent at or below the cutoff leaves its contraction and becomes a shell
+of its own (the compact primitives stay together), as the reference's
+_optimize_contraction does for its J/K optimizer (gpu4pyscf/gto/mole.py:
+1157-1251, diffuse_cutoff=0.3 in gpu4pyscf/scf/jk.py:426): the pieces get
+their own Schwarz factors, so pairs of compact pieces on distant atoms are
+screened out instead of being kept alive by a diffuse tail.  The map between the user basis (spherical or
 Cartesian, any shell order) and this basis is the matrix C with
     D_sorted = C D_user C^T,     V_user = C^T V_sorted C,
 which plays the role of SortedGTO.apply_C_mat_CT / apply_CT_mat_C
@@ -19,21 +25,39 @@ import numpy as np
 from .mole import cart2sph_coeff, common_fac_sp, ncart
 
 
+# exponent at or below which a primitive becomes a shell of its own (the
+# reference's J/K optimizer value)
+DIFFUSE_CUTOFF = 0.3
+
+
 class SortedBasis:
-    def __init__(self, mol):
+    def __init__(self, mol, diffuse_cutoff=None):
         self.mol = mol
+        cutoff = DIFFUSE_CUTOFF if diffuse_cutoff is None else float(diffuse_cutoff)
+        self.diffuse_cutoff = cutoff
         atm = np.asarray(mol._atm, dtype=np.int32)
         bas = np.asarray(mol._bas, dtype=np.int32)
         env = np.asarray(mol._env, dtype=np.float64)
         cart = bool(getattr(mol, 'cart', False))
-        # split general contractions: one (user shell, contraction) entry each
+        # split general contractions: one (user shell, contraction) entry
+        # each, or with the cutoff one for the compact primitives of the
+        # contraction and one per diffuse primitive; the user function is
+        # the sum of its pieces
         entries = []
         for ib in range(len(bas)):
             l, nprim, nctr = int(bas[ib, 1]), int(bas[ib, 2]), int(bas[ib, 3])
+            exps_all = env[bas[ib, 5]: bas[ib, 5] + nprim]
             for k in range(nctr):
                 coef = env[bas[ib, 6] + k * nprim: bas[ib, 6] + (k + 1) * nprim]
                 keep = np.nonzero(coef != 0)[0]
-                entries.append((l, -len(keep), ib, k, keep))
+                if cutoff > 0:
+                    compact = keep[exps_all[keep] > cutoff]
+                    pieces = ([compact] if len(compact) else []) + \
+                        [keep[t:t + 1] for t in np.nonzero(exps_all[keep] <= cutoff)[0]]
+                else:
+                    pieces = [keep]
+                for piece in pieces:
+                    entries.append((l, -len(piece), ib, k, piece))
         order = sorted(range(len(entries)), key=lambda t: (entries[t][0], entries[t][1], t))
         new_env = list(env[:20])
         atm_s = atm.copy()

@@ -40,9 +40,12 @@ class _VHFOpt:
     """Screening optimizer: sorted basis, Schwarz factors, pair lists and the
     device workspace of the engine (gpu4pyscf/scf/jk.py:407-442)."""
 
-    def __init__(self, mol, direct_scf_tol=1e-13, tile=None):
+    def __init__(self, mol, direct_scf_tol=1e-13, tile=None, diffuse_cutoff=None):
         self.mol = mol
         self.direct_scf_tol = direct_scf_tol
+        # primitives with exponents at or below it become shells of their
+        # own in the sorted basis (None: the package default)
+        self.diffuse_cutoff = diffuse_cutoff
         self.h_shls = []
         self.tile = tile
         self.sorted_mol = None
@@ -74,7 +77,7 @@ class _VHFOpt:
 
     def build(self, group_size=None, verbose=None):
         self._free()
-        smol = self.sorted_mol = SortedBasis(self.mol)
+        smol = self.sorted_mol = SortedBasis(self.mol, self.diffuse_cutoff)
         if smol.lmax > LMAX:
             raise NotImplementedError(
                 'shells with l > %d are not supported by the GB300 kernels' % LMAX)

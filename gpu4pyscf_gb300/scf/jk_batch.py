@@ -23,9 +23,10 @@ from .jk import LMAX
 
 
 class BatchJK:
-    def __init__(self, mols, direct_scf_tol=1e-13):
+    def __init__(self, mols, direct_scf_tol=1e-13, diffuse_cutoff=None):
         self.mols = list(mols)
         self.direct_scf_tol = direct_scf_tol
+        self.diffuse_cutoff = diffuse_cutoff
         self.precision = 'fp64'
         self.split_thresh = 1e-6
         self._handle = None
@@ -33,7 +34,7 @@ class BatchJK:
         self.build()
 
     def build(self):
-        self.sorted = [SortedBasis(m) for m in self.mols]
+        self.sorted = [SortedBasis(m, self.diffuse_cutoff) for m in self.mols]
         for sb in self.sorted:
             if sb.lmax > LMAX:
                 raise NotImplementedError('shells with l > %d are not supported' % LMAX)

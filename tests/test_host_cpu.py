@@ -45,6 +45,43 @@ def test_sorted_basis_transform(cart):
     assert abs(vk - vk0).max() < 1e-10
 
 
+@pytest.mark.parametrize('cart', [False, True])
+def test_diffuse_primitives_peeled(cart):
+    """Primitives at or below the cutoff leave their contraction as shells of
+    their own (gpu4pyscf/gto/mole.py:1157-1251): a 4-primitive s and a
+    general p contraction with diffuse members split into compact and
+    single-primitive shells, and J/K through the split basis equal the
+    user-basis J/K."""
+    extra = [[0, [10., .3], [1., .5], [.2, .4], [.05, .2]],
+             [1, [3., .4, .1], [.8, .5, .3], [.25, .3, .8]]]
+    mol = gto.M(atom='O 0 0 0.1174; H -0.757 0 -0.4696; H 0.757 0 -0.4696',
+                basis=('syn-6-31g*', extra), cart=cart)
+    sb0 = SortedBasis(mol, 0.)
+    sb = SortedBasis(mol, 0.3)
+    # one shell per contraction's compact part plus one per diffuse primitive
+    expect = 0
+    for bb in np.asarray(mol._bas):
+        e = mol._env[bb[5]:bb[5] + bb[2]]
+        for k in range(bb[3]):
+            c = mol._env[bb[6] + k * bb[2]:bb[6] + (k + 1) * bb[2]]
+            expect += int(np.any((e > .3) & (c != 0))) + int(np.sum((e <= .3) & (c != 0)))
+    assert sb.nbas == expect > sb0.nbas + mol.natm * (2 + 2) - 1
+    assert np.all(sb._bas[:, 3] == 1)
+    exps = [sb._env[b[5]:b[5] + b[2]] for b in sb._bas]
+    assert all(len(e) == 1 or np.all(e > 0.3) for e in exps)
+    rng = np.random.default_rng(3)
+    dm = rng.random((mol.nao, mol.nao)) - .5
+    dm = dm + dm.T
+    vj0, vk0 = orc.get_jk(mol, dm, hermi=1)
+    C = sb.coeff
+
+    class Raw:
+        _atm, _bas, _env = sb._atm, sb._bas, sb._env
+    vj_s, vk_s, _ = orc.get_jk_cart(Raw, C @ dm @ C.T, hermi=1)
+    assert abs(C.T @ vj_s @ C - vj0).max() < 1e-10
+    assert abs(C.T @ vk_s @ C - vk0).max() < 1e-10
+
+
 def test_basis_parsing_forms():
     m1 = gto.M(atom='C 0 0 0', basis=('sto-3g', [[3, [1.4, 1.]]]))
     assert list(m1._bas[:, 1]) == [0, 0, 1, 3]
