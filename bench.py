@@ -530,17 +530,16 @@ def run_profile(args):
 
 def run_grad(args):
     """bench.py --mode grad: nuclear gradient of the J/K energy of --config
-    (SAD density, j_factor 1, k_factor 0.5) through the dedicated derivative
-    kernels, timed with CUDA events (3 untimed, 5 timed), beside the route
-    through the J/K kernels of the extended basis (timed twice) and their
-    agreement; then one more gradient inside the NVTX range 'grad_profile'."""
+    (j_factor 1, k_factor 0.5) for the SAD density and for the dense density
+    after the first SCF step, through the dedicated derivative kernels, timed
+    with CUDA events (3 untimed, 5 timed), beside the route through the J/K
+    kernels of the extended basis (1 untimed, 2 timed) and their agreement;
+    then one more dense-density gradient inside the NVTX range
+    'grad_profile'."""
     import torch
     from gpu4pyscf_gb300.scf import grad_jk, jk
     mol = make_mol(args.config)
-    dm = make_density(mol)
     opt = jk._VHFOpt(mol, direct_scf_tol=1e-13).build()
-    st = {}
-    g1 = grad_jk.jk_energy_grad(mol, dm, 1., .5, vhfopt=opt, stats=st)
 
     def timed(fn, n):
         ts = []
@@ -553,25 +552,31 @@ def run_grad(args):
             torch.cuda.synchronize()
             ts.append(e0.elapsed_time(e1) * 1e-3)
         return sorted(ts)
-    for _ in range(3):
-        grad_jk.jk_energy_grad(mol, dm, 1., .5, vhfopt=opt)
-    t_ip1 = timed(lambda: grad_jk.jk_energy_grad(mol, dm, 1., .5, vhfopt=opt), 5)
-    g2 = grad_jk.jk_energy_grad(mol, dm, 1., .5, method='extended')
-    t_ext = timed(lambda: grad_jk.jk_energy_grad(mol, dm, 1., .5, method='extended'), 2)
-    torch.cuda.synchronize()
-    nvtx_push('grad_profile')
-    grad_jk.jk_energy_grad(mol, dm, 1., .5, vhfopt=opt)
-    torch.cuda.synchronize()
-    nvtx_pop()
-    d = (g1 - g2).abs().max().item()
-    print(json.dumps({'mode': 'grad', 'config': CONFIGS[args.config]['workload'], 'density': 'SAD',
-                      'j_factor': 1., 'k_factor': .5, 'natm': mol.natm,
-                      's_per_grad_ip1': t_ip1, 's_per_grad_extended': t_ext,
+    dms = {'SAD': make_density(mol), 'dense': dense_density(mol)[0]}
+    rows = {}
+    for name, dm in dms.items():
+        st = {}
+        g1 = grad_jk.jk_energy_grad(mol, dm, 1., .5, vhfopt=opt, stats=st)
+        for _ in range(3):
+            grad_jk.jk_energy_grad(mol, dm, 1., .5, vhfopt=opt)
+        t_ip1 = timed(lambda: grad_jk.jk_energy_grad(mol, dm, 1., .5, vhfopt=opt), 5)
+        g2 = grad_jk.jk_energy_grad(mol, dm, 1., .5, method='extended')
+        t_ext = timed(lambda: grad_jk.jk_energy_grad(mol, dm, 1., .5, method='extended'), 2)
+        rows[name] = {'s_per_grad_ip1': t_ip1, 's_per_grad_extended': t_ext,
                       'speedup_ip1_vs_extended': t_ext[0] / t_ip1[0], 'quartets': st.get('quartets'),
                       'prim_quartets': st.get('prim_quartets'),
                       'quartets_per_s': st.get('quartets', 0) / t_ip1[0],
-                      'max_abs_diff_ip1_vs_extended': d, 'max_abs_grad': g2.abs().max().item(),
-                      'translational_sum': g1.sum(0).abs().max().item()}))
+                      'prim_quartets_per_s': st.get('prim_quartets', 0) / t_ip1[0],
+                      'max_abs_diff_ip1_vs_extended': (g1 - g2).abs().max().item(),
+                      'max_abs_grad': g2.abs().max().item(),
+                      'translational_sum': g1.sum(0).abs().max().item()}
+    torch.cuda.synchronize()
+    nvtx_push('grad_profile')
+    grad_jk.jk_energy_grad(mol, dms['dense'], 1., .5, vhfopt=opt)
+    torch.cuda.synchronize()
+    nvtx_pop()
+    print(json.dumps({'mode': 'grad', 'config': CONFIGS[args.config]['workload'], 'j_factor': 1., 'k_factor': .5,
+                      'natm': mol.natm, 'densities': rows}))
 
 
 def run_guess(args):
