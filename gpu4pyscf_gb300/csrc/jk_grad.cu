@@ -66,9 +66,15 @@ __host__ __device__ __forceinline__ int gr_box(int li, int lj, int lk, int ll) {
 __host__ __device__ __forceinline__ int gr_nroots(int li, int lj, int lk, int ll) {
     return (li + lj + lk + ll + 1) / 2 + 1;
 }
-__host__ __device__ __forceinline__ int gr_slot_doubles(int li, int lj, int lk, int ll) {
+__host__ __device__ __forceinline__ int gr_obox(int li, int lj, int lk, int ll) {
+    return (li + 1) * (lj + 1) * (lk + 1) * (ll + 1);
+}
+// doubles per slot: the raised boxes, with der the derivative arrays
+// (integral and its A, B, C derivatives over the class's own index box),
+// roots and weights, scalars
+__host__ __device__ __forceinline__ int gr_slot_doubles(int li, int lj, int lk, int ll, bool der) {
     const int nr = gr_nroots(li, lj, lk, ll);
-    return nr * 3 * gr_box(li, lj, lk, ll) + 2 * nr + GR_NSC;
+    return nr * 3 * gr_box(li, lj, lk, ll) + (der ? nr * 12 * gr_obox(li, lj, lk, ll) : 0) + 2 * nr + GR_NSC;
 }
 
 // Screening of a quartet for the gradient: q_ij q_kl times the largest
@@ -89,7 +95,13 @@ __device__ __forceinline__ bool grad_passes(const EngineDev &d, const GradDev &g
 
 }  // namespace
 
-template <int NR>
+// DER: after the raised boxes one more stage (S2b, every thread) forms the
+// derivative arrays G, dA, dB, dC of each (slot, root, axis) over the
+// class's own index box, so that the element stage needs 15 FP64
+// instructions per element and root instead of 33; classes whose arrays
+// do not fit the shared-memory budget (pairs of f shells) take the
+// derivatives from the raised box inside the element stage.
+template <int NR, bool DER>
 __global__ void __launch_bounds__(JK_THREADS, GRAD_MIN_BLOCKS)
 rys_ip1_kernel(EngineDev d, ClassDev c, GradDev gd)
 {
@@ -99,7 +111,11 @@ rys_ip1_kernel(EngineDev d, ClassDev c, GradDev gd)
     const int ijm = li + lj + 1, klm = lk + ll + 1;
     // raised box of one (root, axis): index a sA + b sB + c sC + d
     const int sC = ll + 1, sB = (lk + 2) * sC, sA = (lj + 2) * sB, box = (li + 2) * sA;
-    const int slot_d = NR * 3 * box + 2 * NR + GR_NSC;
+    // the class's own index box: index ((a (lj+1) + b) (lk+1) + c) (ll+1) + d
+    const int oC = ll + 1, oB = (lk + 1) * oC, oA = (lj + 1) * oB, obox = (li + 1) * oA;
+    const int qoff = NR * 3 * box;                              // derivative arrays
+    const int rwoff = qoff + (DER ? NR * 12 * obox : 0);        // roots, weights, scalars
+    const int slot_d = rwoff + 2 * NR + GR_NSC;
     const int qb = gd.qb, tps = JK_THREADS / qb;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     double *sm = reinterpret_cast<double *>(smem_raw);   // [qb][slot_d]
@@ -189,12 +205,19 @@ rys_ip1_kernel(EngineDev d, ClassDev c, GradDev gd)
                         gr_cart(lj, bb, bx, by, bz);
                         gr_cart(lk, cc, cx, cy, cz);
                         gr_cart(ll, dd, dx, dy, dz);
-                        const int ix = ax * sA + bx * sB + cx * sC + dx;
-                        const int iy = ay * sA + by * sB + cy * sC + dy;
-                        const int iz = az * sA + bz * sB + cz * sC + dz;
-                        ix3[mm] = ix | (iy << 10) | (iz << 20);
-                        ex9[mm] = ax | (ay << 3) | (az << 6) | (bx << 9) | (by << 12) | (bz << 15) |
-                                  (cx << 18) | (cy << 21) | (cz << 24);
+                        if (DER) {
+                            const int ox = ax * oA + bx * oB + cx * oC + dx;
+                            const int oy = ay * oA + by * oB + cy * oC + dy;
+                            const int oz = az * oA + bz * oB + cz * oC + dz;
+                            ix3[mm] = ox | (oy << 10) | (oz << 20);
+                        } else {
+                            const int ix = ax * sA + bx * sB + cx * sC + dx;
+                            const int iy = ay * sA + by * sB + cy * sC + dy;
+                            const int iz = az * sA + bz * sB + cz * sC + dz;
+                            ix3[mm] = ix | (iy << 10) | (iz << 20);
+                            ex9[mm] = ax | (ay << 3) | (az << 6) | (bx << 9) | (by << 12) | (bz << 15) |
+                                      (cx << 18) | (cy << 21) | (cz << 24);
+                        }
                         const size_t i = A.ao + aa, j = B.ao + bb;
                         const size_t k = d.shells[s_k[slot]].ao + cc, l = d.shells[s_l[slot]].ao + dd;
                         double js_ij = 0., js_kl = 0., kx = 0.;
@@ -217,7 +240,7 @@ rys_ip1_kernel(EngineDev d, ClassDev c, GradDev gd)
                     for (int t = tid; t < nb * NR; t += JK_THREADS) {
                         const int s = t / NR, r = t - s * NR;
                         double *sl = sm + s * slot_d;
-                        double *rw = sl + NR * 3 * box;
+                        double *rw = sl + rwoff;
                         double *sc = rw + 2 * NR;
                         const int pb = pb_off + step / npk, pk = s_pk[s] + step % npk;
                         const d4 a1 = d.pp_a[pb], a2 = d.pp_a[pk];
@@ -250,7 +273,7 @@ rys_ip1_kernel(EngineDev d, ClassDev c, GradDev gd)
                     for (int t = tid; t < nb * NR * 3; t += JK_THREADS) {
                         const int s = t / (NR * 3), r = (t / 3) % NR, ax = t % 3;
                         double *sl = sm + s * slot_d;
-                        const double *rw = sl + NR * 3 * box;
+                        const double *rw = sl + rwoff;
                         const double *sc = rw + 2 * NR;
                         double *gq = sl + (r * 3 + ax) * box;
                         const double u = rw[r];
@@ -300,10 +323,57 @@ rys_ip1_kernel(EngineDev d, ClassDev c, GradDev gd)
                             }
                     }
                     __syncthreads();
+                    if (DER) {
+                        // ---- S2b: derivative arrays of every (slot, root,
+                        // axis): G, 2 a_i G(a+1) - a G(a-1), and the same
+                        // for b and c
+                        const int per = NR * 3 * obox;
+                        for (int t = tid; t < nb * per; t += JK_THREADS) {
+                            const int s = t / per, rem = t - s * per;
+                            const int ra = rem / obox, o = rem - ra * obox;
+                            const int dd = o % oC, t1 = o / oC;
+                            const int cc = t1 % (lk + 1), t2 = t1 / (lk + 1);
+                            const int bb = t2 % (lj + 1), aa = t2 / (lj + 1);
+                            double *sl = sm + s * slot_d;
+                            const double *sc = sl + rwoff + 2 * NR;
+                            const double *R = sl + ra * box;
+                            double *Q = sl + qoff + ra * 4 * obox;
+                            const int ri = aa * sA + bb * sB + cc * sC + dd;
+                            Q[o] = R[ri];
+                            Q[obox + o] = fma(sc[20], R[ri + sA], -aa * R[ri - (aa ? sA : 0)]);
+                            Q[2 * obox + o] = fma(sc[21], R[ri + sB], -bb * R[ri - (bb ? sB : 0)]);
+                            Q[3 * obox + o] = fma(sc[22], R[ri + sC], -cc * R[ri - (cc ? sC : 0)]);
+                        }
+                        __syncthreads();
+                    }
                     // ---- S3: this thread's elements, nine derivative sums
-                    if (active) {
+                    if (active && DER) {
+                        const double *Qs = sm + slot * slot_d + qoff;
+#pragma unroll
+                        for (int mm = 0; mm < GR_EPT; ++mm) {
+                            if (W[mm] == 0.) continue;
+                            const int ox = ix3[mm] & 1023, oy = (ix3[mm] >> 10) & 1023, oz = ix3[mm] >> 20;
+                            const double wgt = W[mm];
+#pragma unroll
+                            for (int r = 0; r < NR; ++r) {
+                                const double *qx = Qs + r * 12 * obox, *qy = qx + 4 * obox, *qz = qy + 4 * obox;
+                                const double X = qx[ox], Y = qy[oy], Z = qz[oz];
+                                const double wyz = wgt * Y * Z, wxz = wgt * X * Z, wxy = wgt * X * Y;
+                                acc[0] = fma(qx[obox + ox], wyz, acc[0]);
+                                acc[1] = fma(qy[obox + oy], wxz, acc[1]);
+                                acc[2] = fma(qz[obox + oz], wxy, acc[2]);
+                                acc[3] = fma(qx[2 * obox + ox], wyz, acc[3]);
+                                acc[4] = fma(qy[2 * obox + oy], wxz, acc[4]);
+                                acc[5] = fma(qz[2 * obox + oz], wxy, acc[5]);
+                                acc[6] = fma(qx[3 * obox + ox], wyz, acc[6]);
+                                acc[7] = fma(qy[3 * obox + oy], wxz, acc[7]);
+                                acc[8] = fma(qz[3 * obox + oz], wxy, acc[8]);
+                            }
+                        }
+                    }
+                    if (active && !DER) {
                         const double *sl = sm + slot * slot_d;
-                        const double *sc = sl + NR * 3 * box + 2 * NR;
+                        const double *sc = sl + rwoff + 2 * NR;
                         const double ai2 = sc[20], aj2 = sc[21], ak2 = sc[22];
 #pragma unroll
                         for (int mm = 0; mm < GR_EPT; ++mm) {
@@ -362,15 +432,16 @@ rys_ip1_kernel(EngineDev d, ClassDev c, GradDev gd)
 
 namespace {
 
+template <bool DER>
 const void *grad_kernel_of(int nr) {
     switch (nr) {
-        case 1: return (const void *)rys_ip1_kernel<1>;
-        case 2: return (const void *)rys_ip1_kernel<2>;
-        case 3: return (const void *)rys_ip1_kernel<3>;
-        case 4: return (const void *)rys_ip1_kernel<4>;
-        case 5: return (const void *)rys_ip1_kernel<5>;
-        case 6: return (const void *)rys_ip1_kernel<6>;
-        case 7: return (const void *)rys_ip1_kernel<7>;
+        case 1: return (const void *)rys_ip1_kernel<1, DER>;
+        case 2: return (const void *)rys_ip1_kernel<2, DER>;
+        case 3: return (const void *)rys_ip1_kernel<3, DER>;
+        case 4: return (const void *)rys_ip1_kernel<4, DER>;
+        case 5: return (const void *)rys_ip1_kernel<5, DER>;
+        case 6: return (const void *)rys_ip1_kernel<6, DER>;
+        case 7: return (const void *)rys_ip1_kernel<7, DER>;
         default: return nullptr;
     }
 }
@@ -381,32 +452,30 @@ int grad_class(int li, int lj, int lk, int ll, GradClass *out) {
     if (li > GRAD_LMAX || lj > GRAD_LMAX || lk > GRAD_LMAX || ll > GRAD_LMAX) return 1;
     const int nr = gr_nroots(li, lj, lk, ll);
     static_assert(GR_NRMAX <= 7, "gradient kernels are instantiated up to 7 roots");
-    const int slot = gr_slot_doubles(li, lj, lk, ll) * (int)sizeof(double);
+    const bool der = gr_slot_doubles(li, lj, lk, ll, true) * (int)sizeof(double) <= GR_SMEM_BUDGET;
+    const int slot = gr_slot_doubles(li, lj, lk, ll, der) * (int)sizeof(double);
     int qb = GR_QBMAX;
     while (qb > 1 && qb * slot > GR_SMEM_BUDGET) qb >>= 1;
-    out->kernel = grad_kernel_of(nr);
+    out->kernel = der ? grad_kernel_of<true>(nr) : grad_kernel_of<false>(nr);
     out->qb = qb;
     out->smem = qb * slot;
     return out->kernel ? 0 : 1;
 }
 
 int grad_set_smem_attrs() {
-    int need[8] = {0};
     for (int li = 0; li <= GRAD_LMAX; ++li)
         for (int lj = 0; lj <= GRAD_LMAX; ++lj)
             for (int lk = 0; lk <= GRAD_LMAX; ++lk)
                 for (int ll = 0; ll <= GRAD_LMAX; ++ll) {
                     GradClass g;
                     if (grad_class(li, lj, lk, ll, &g)) continue;
-                    const int nr = gr_nroots(li, lj, lk, ll);
-                    need[nr] = need[nr] > g.smem ? need[nr] : g.smem;
+                    cudaFuncAttributes fa;
+                    cudaError_t e = cudaFuncGetAttributes(&fa, g.kernel);
+                    if (e != cudaSuccess) return (int)e;
+                    if (fa.maxDynamicSharedSizeBytes >= g.smem) continue;
+                    e = cudaFuncSetAttribute(g.kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, g.smem);
+                    if (e != cudaSuccess) return (int)e;
                 }
-    for (int nr = 1; nr < 8; ++nr) {
-        if (!need[nr]) continue;
-        const cudaError_t e = cudaFuncSetAttribute(grad_kernel_of(nr), cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                                   need[nr]);
-        if (e != cudaSuccess) return (int)e;
-    }
     return 0;
 }
 
