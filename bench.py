@@ -15,7 +15,8 @@ Printed JSON line (one per run, rank 0):
               over FP64 and the error against the FP64 build, and a sweep
               of splits 1e-8 .. 1e-2;
   mixed_dense FP64 vs mixed (splits 1e-6, 1e-4) for a dense SCF density of
-              the same molecule (the first SCF step from SAD);
+              the same molecule (the first SCF step from SAD), and the
+              nuclear gradient of the J/K energy of that density;
   roofline    the dominant class kernel: algorithmic FP64 FLOP/s against the
               FP64 FMA peak measured here by an FMA-chain probe;
   cpu_baseline  the C++ CPU oracle on this host's cores on a bounded sample.
@@ -630,14 +631,15 @@ def dense_density(mol, host_eig=False):
     return mf.make_rdm1(c, mf.get_occ(e, c)), mf
 
 
-def dense_mixed(mol, splits=(1e-6, 1e-4)):
+def dense_mixed(mol, splits=(1e-6, 1e-4), grad_out=None):
     """J/K of a dense SCF density of mol (the density after the first SCF
     step from SAD, what every later Fock build of an SCF sees), FP64 against
     mixed at the given splits: seconds per build (CUDA events, after one
     warm-up build each), speed-up, max |dJ|, |dK| and the two-electron energy
     change.  The SAD density of the default benchmark is block diagonal by
     atom, which the density screening exploits; this is the build of the SCF
-    iterations."""
+    iterations.  grad_out (a dict): also time the nuclear gradient of the
+    J/K energy of that density into it."""
     import torch
     from gpu4pyscf_gb300.scf import jk
     dm, mf = dense_density(mol)
@@ -662,6 +664,24 @@ def dense_mixed(mol, splits=(1e-6, 1e-4)):
                      'max_abs_dK': float((vk - ref[1]).abs().max()), 'dE_2e_Ha': de})
         print(json.dumps(rows[-1]), file=sys.stderr, flush=True)
     opt.precision = 'fp64'
+    if grad_out is not None:
+        # nuclear gradient of the J/K energy (j 1, k 0.5) of the same
+        # density through the derivative kernels: one untimed, two timed
+        from gpu4pyscf_gb300.scf import grad_jk
+        st = {}
+        g = grad_jk.jk_energy_grad(mol, dm, 1., .5, vhfopt=opt, stats=st)
+        ts = []
+        for _ in range(2):
+            torch.cuda.synchronize()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record()
+            grad_jk.jk_energy_grad(mol, dm, 1., .5, vhfopt=opt)
+            e1.record()
+            torch.cuda.synchronize()
+            ts.append(e0.elapsed_time(e1) * 1e-3)
+        grad_out.update({'s_per_grad': min(ts), 'quartets': st['quartets'], 'prim_quartets': st['prim_quartets'],
+                         'prim_quartets_per_s': st['prim_quartets'] / min(ts),
+                         'translational_sum': g.sum(0).abs().max().item(), 'max_abs_grad': g.abs().max().item()})
     return rows
 
 
@@ -870,8 +890,11 @@ def run_gpu(args):
 
     # mixed precision on the density an SCF iteration sees (dense), next to
     # the SAD-density numbers above; reported, never fatal to the line
+    grad_dense = {'what': 'nuclear gradient of the J/K energy (j 1, k 0.5) of the same dense density, '
+                          'derivative kernels (jk_energy_grad)'}
     try:
-        mixed_dense = {'density': 'first SCF step from SAD (dense)', 'runs': dense_mixed(mol)}
+        mixed_dense = {'density': 'first SCF step from SAD (dense)', 'runs': dense_mixed(mol, grad_out=grad_dense)}
+        mixed_dense['grad'] = grad_dense
     except Exception as exc:  # noqa: BLE001
         mixed_dense = {'error': '%s: %s' % (type(exc).__name__, exc)}
 
