@@ -14,6 +14,7 @@ Printed JSON line (one per run, rank 0):
   mixed       the mixed FP32/FP64 build at split 1e-6: quartets/s, speed-up
               over FP64 and the error against the FP64 build, and a sweep
               of splits 1e-8 .. 1e-2;
+  j_only      the J-only build of the same density (Coulomb-block screening);
   mixed_dense FP64 vs mixed (splits 1e-6, 1e-4) for a dense SCF density of
               the same molecule (the first SCF step from SAD), and the
               nuclear gradient of the J/K energy of that density;
@@ -25,7 +26,8 @@ Printed JSON line (one per run, rank 0):
 restatement of PySCF's get_jk) on all host cores for the same workload.
 --mode scf runs a full RHF of --config (FP64 and mixed J/K); --mode dense
 times FP64 against mixed J/K on a dense SCF density of --config (c120: the
-120-atom molecule).
+120-atom molecule); --mode grad times the nuclear gradient of the J/K
+energy; --mode profile and --mode guess as their help says.
 """
 import argparse
 import ctypes
@@ -403,8 +405,8 @@ def kernel_family(li, lj, lk, ll):
 # build, from one ncu capture of the c30 command (--set full, one launch of
 # the class inside the 'jk_timed' NVTX range); the roofline's traffic when
 # the dominant class is among them
-# DRAM read + write bytes of one launch of a class, from the full ncu captures
-# summarised in profiles/rys_fp64_kernels_c30.md (commands there)
+# DRAM read + write bytes of one launch of a class, from a full ncu capture
+# of that launch in this code (`--mode profile`, NVTX range jk_profile)
 NCU_DRAM_BYTES = {('c30', '(11|11)'): 1685760 + 5376, ('c30', '(11|10)'): 3351808}
 
 
@@ -795,6 +797,23 @@ def run_gpu(args):
     mixed['sweep'] = {'columns': ['split', 'precision', 's_per_jk_build', 'speedup_vs_fp64',
                                   'max_abs_dJ', 'max_abs_dK', 'dE_2e_Ha'], 'rows': sweep}
 
+    # J-only build of the same density: the J engine's screening (the
+    # Coulomb blocks D_ij, D_kl only) on the same kernels with K off;
+    # reported, never fatal to the line
+    try:
+        opt._build(dms, 1, True, False, stats=True)
+        stj = dict(opt.last_stats)
+        build_j = lambda: opt._build(dms, 1, True, False)
+        for _ in range(2):
+            build_j()
+        tj = sum(timed(build_j, args.steps)) / args.steps
+        vjj, _ = opt._build(dms, 1, True, False)
+        j_only = {'s_per_j_build': tj, 'quartets': stj['quartets_fp64'],
+                  'quartets_per_s': stj['quartets_fp64'] / tj, 'speedup_vs_jk_build': t64s / tj,
+                  'max_abs_dJ_vs_jk_build': float(abs(vjj[0] - vj64[0]).max().item())}
+    except Exception as exc:  # noqa: BLE001
+        j_only = {'error': '%s: %s' % (type(exc).__name__, exc)}
+
     # per-class kernel times (CUDA events on the build stream) for the roofline
     h = opt._handle
     lib.jk_opt_time_classes(h, 1)
@@ -850,8 +869,8 @@ def run_gpu(args):
     traffic = NCU_DRAM_BYTES.get((args.config, dom['class']))
     roofline = {'bound': 'fp64', 'achieved': achieved, 'peak': peak64 / 1e12, 'unit': 'TFLOP/s',
                 'frac': achieved / (peak64 / 1e12), 'traffic': traffic,
-                'traffic_source': ('DRAM read + write of one launch of this class from the full ncu capture '
-                                   'in profiles/rys_fp64_kernels_c30.md (same code), not measured in this '
+                'traffic_source': ('DRAM read + write of one launch of this class from a full ncu capture '
+                                   'of bench.py --mode profile (same code), not measured in this '
                                    'run' if traffic else None),
                 'kernel': '%s %s FP64' % (kernel_family(*lk4), dom['class']), 'dominant': dom,
                 'peak_source': 'FP64 FMA-chain probe measured in this run (MEASURED_PEAKS.json has no FP64 figure)',
@@ -929,7 +948,7 @@ def run_gpu(args):
                 'e2e': {'value': e2e_val, 'unit': 'quartets/s', 'h2d_bytes_per_step': nbytes,
                         'd2h_bytes_per_step': 2 * nbytes, 's_per_step': sum(te) / args.steps},
                 'gpu_launches': int(st64['kernel_launches']) * args.steps,
-                'mixed': mixed, 'mixed_dense': mixed_dense, 'roofline': roofline, 'classes_top': per_class[:8],
+                'mixed': mixed, 'j_only': j_only, 'mixed_dense': mixed_dense, 'roofline': roofline, 'classes_top': per_class[:8],
                 'batched': batched, 'cpu_baseline': cpu, 'parity': parity, 'clocks': clock_info}
         print(json.dumps(line))
     if world > 1:

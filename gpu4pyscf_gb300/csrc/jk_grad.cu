@@ -19,12 +19,14 @@
 // Work layout.  A block of 256 threads takes a work unit (one bra pair and
 // up to 64 kets of one primitive-count bucket), screens its kets and works
 // on the passing quartets qb at a time ("slots", qb per class so that the
-// slots' raised boxes fit in shared memory).  Quartets of a unit share the
-// bra pair and the primitive counts, so the slots walk their primitive
-// quartets in lockstep: per step one thread per (slot, root) evaluates a
-// root and weight (S1), one thread per (slot, root, axis) the raised box (S2), and
-// the 256/qb threads of a slot their share of the slot's Cartesian elements
-// (S3), each holding the density weights of its elements in registers.
+// slots' shared-memory arrays fit).  Quartets of a unit share the bra pair
+// and the primitive counts, so the slots walk their primitive quartets in
+// lockstep: per step one thread per (slot, root) evaluates a root and
+// weight (S1), one thread per (slot, root, axis) the raised box (S2), every
+// thread a share of the derivative arrays (S2b, see rys_ip1_kernel), and
+// the 256/qb threads of a slot their share of the slot's Cartesian
+// elements (S3), each holding the density weights of its elements in
+// registers.
 #include "jk_device.cuh"
 #include "jk_registry.h"
 #include "rys_roots.cuh"

@@ -117,6 +117,8 @@ def test_bad_arguments_rejected_without_gpu():
     assert lib.jk_opt_create(None, 0, None, 0, None, 0, 1e-13, 0, ctypes.byref(h)) == -1
     assert b'invalid' in lib.jk_last_error()
     assert lib.jk_build(None, None, 1, 1, 1, 1, 1, 0, 0., None, None, None, None) == -1
+    assert lib.jk_energy_grad(None, None, 1, 1, 1., 1., 0., 1., 1., None, None, None) == -1
+    assert lib.jk_opt_natm(None) == -1
 
 
 def _header_arity(path):
