@@ -18,6 +18,12 @@
  *   jk_opt_destroy  release of the GPU caches held by _VHFOpt (jk.py:418-421)
  *   jk_last_error   the stderr message + int status of RYS_build_jk
  *                   (rys_contract_jk.cu:442-452)
+ *   jk_energy_grad  RYS_per_atom_jk_ip1 (lib/gvhf-rys/rys_contract_jk_ip1.cu:
+ *                   1747-1797) and the class loop of _jk_energy_per_atom
+ *                   (grad/rhf.py:60-171)
+ * The remaining entry points (batched builds, range separation, the
+ * allocation-free build, autotuning, deterministic accumulation) say at
+ * their declaration what they replace or that the reference has none.
  */
 #ifndef GB300JK_H
 #define GB300JK_H
