@@ -285,6 +285,42 @@ __global__ void fx_to_double_kernel(const unsigned long long *fx, size_t n, doub
         out[x] = (double)(long long)fx[2 * x] * (1. / JK_FX_HI) + (double)(long long)fx[2 * x + 1] * (1. / JK_FX_LO);
 }
 
+// Products with the sparse map C between the user and the sorted basis
+// (each row holds the few coefficients of one Cartesian component: a
+// Cartesian-to-spherical block or a scale factor), S given as compressed
+// rows (ptr, idx, val):
+//   right: out[i][r][m] = sum_p in[i][r][idx[p]] val[p],  p in row m of S
+//   left:  out[i][r][m] = sum_p val[p] in[i][idx[p]][m],  p in row r of S
+// so that C D C^T is right then left with S = C, and C^T V C right then
+// left with S = C^T.  A dense product spends O(nao^3) FP64 operations on
+// zeros (GB300's FP64 rate makes that milliseconds at nao ~ 700); these
+// spend a few per element.
+__global__ void sparse_right_kernel(const int *ptr, const int *idx, const double *val, long long total, int K, int M,
+                                    const double *in, double *out) {
+    for (long long x = blockIdx.x * (long long)blockDim.x + threadIdx.x; x < total;
+         x += (long long)gridDim.x * blockDim.x) {
+        const int m = (int)(x % M);
+        const double *row = in + (x / M) * K;
+        double s = 0.;
+        for (int p = __ldg(ptr + m); p < __ldg(ptr + m + 1); ++p) s = fma(row[__ldg(idx + p)], __ldg(val + p), s);
+        out[x] = s;
+    }
+}
+
+__global__ void sparse_left_kernel(const int *ptr, const int *idx, const double *val, long long total, int R, int K,
+                                   int M, const double *in, double *out) {
+    for (long long x = blockIdx.x * (long long)blockDim.x + threadIdx.x; x < total;
+         x += (long long)gridDim.x * blockDim.x) {
+        const int m = (int)(x % M);
+        const long long ir = x / M;
+        const int r = (int)(ir % R);
+        const double *blk = in + (ir / R) * K * (long long)M;
+        double s = 0.;
+        for (int p = __ldg(ptr + r); p < __ldg(ptr + r + 1); ++p) s = fma(__ldg(val + p), blk[(long long)__ldg(idx + p) * M + m], s);
+        out[x] = s;
+    }
+}
+
 __global__ void epilogue_kernel(const double *jt, const double *kt, int n_dm, Layout L, int hermi,
                                 int with_j, int with_k, double *vj, double *vk) {
     const size_t nn = (size_t)L.ntot;
@@ -1314,6 +1350,21 @@ int jk_energy_grad(jk_opt *o, const double *dm, int n_dm, int nao, double j_fact
 }
 
 int jk_opt_natm(const jk_opt *opt) { return opt ? opt->natm : -1; }
+
+int jk_sparse_mm(int side, const int *ptr, const int *idx, const double *val, int n, int R, int K, int M,
+                 const double *in, double *out, void *stream) {
+    if ((side != 0 && side != 1) || !ptr || !idx || !val || !in || !out || n <= 0 || R <= 0 || K <= 0 || M <= 0)
+        return fail(JK_ERR_ARG, "jk_sparse_mm: invalid arguments");
+    cudaStream_t st = (cudaStream_t)stream;
+    const long long total = (long long)n * R * M;
+    const int grid = (int)std::min<long long>((total + 255) / 256, 4096);
+    if (side == 0)
+        sparse_right_kernel<<<grid, 256, 0, st>>>(ptr, idx, val, total, K, M, in, out);
+    else
+        sparse_left_kernel<<<grid, 256, 0, st>>>(ptr, idx, val, total, R, K, M, in, out);
+    CK(cudaGetLastError());
+    return 0;
+}
 
 int jk_opt_set_mol_ndm(jk_opt *o, const int32_t *ndm) {
     if (!o) return fail(JK_ERR_ARG, "jk_opt_set_mol_ndm: null optimizer");

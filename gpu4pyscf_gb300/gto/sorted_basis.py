@@ -112,3 +112,15 @@ class SortedBasis:
 
     def ao_loc_nr(self):
         return self.ao_loc
+
+    def coeff_rows(self, transpose=False):
+        """Compressed rows (ptr, idx, val) of C (rows: sorted AOs, idx: user
+        AOs) or, with transpose, of C^T (rows: user AOs, idx: sorted AOs):
+        the few nonzeros of each row, for the sparse products of the C
+        transforms."""
+        M = self.coeff.T if transpose else self.coeff
+        rows, cols = np.nonzero(M)
+        ptr = np.zeros(M.shape[0] + 1, dtype=np.int32)
+        np.add.at(ptr, rows + 1, 1)
+        ptr = np.cumsum(ptr).astype(np.int32)
+        return ptr, cols.astype(np.int32), np.ascontiguousarray(M[rows, cols], dtype=np.float64)

@@ -39,7 +39,7 @@ EXPORTS = ('jk_opt_create', 'jk_opt_destroy', 'jk_opt_nao', 'jk_opt_npairs',
            'jk_opt_time_classes', 'jk_opt_class_times', 'jk_probe_fma', 'jk_int1e',
            'jk_int1e_last_error', 'jk_opt_create_batch', 'jk_build_batch', 'jk_opt_ntot',
            'jk_opt_tune', 'jk_opt_set_variant', 'jk_opt_get_variant', 'jk_opt_set_mol_ndm',
-           'jk_build_rsh', 'jk_opt_set_deterministic', 'jk_energy_grad', 'jk_opt_natm')
+           'jk_build_rsh', 'jk_opt_set_deterministic', 'jk_energy_grad', 'jk_opt_natm', 'jk_sparse_mm')
 
 
 def load(path=None):
@@ -106,6 +106,8 @@ def load(path=None):
         lib.jk_energy_grad.restype = i32
         lib.jk_opt_natm.argtypes = [vp]
         lib.jk_opt_natm.restype = i32
+        lib.jk_sparse_mm.argtypes = [i32, vp, vp, vp, i32, i32, i32, i32, vp, vp, vp]
+        lib.jk_sparse_mm.restype = i32
         _lib = lib
         return lib
 

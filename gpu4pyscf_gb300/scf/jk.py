@@ -94,6 +94,9 @@ class _VHFOpt:
         self._handle = h
         self._det_set = False
         self._coeff = torch.as_tensor(smol.coeff, device='cuda')
+        # compressed rows of C and C^T for the sparse transforms
+        self._c_rows = tuple(torch.as_tensor(a, device='cuda') for a in smol.coeff_rows())
+        self._ct_rows = tuple(torch.as_tensor(a, device='cuda') for a in smol.coeff_rows(transpose=True))
         return self
 
     @property
@@ -126,22 +129,46 @@ class _VHFOpt:
                 for k, v in out.items()}
 
     # -- basis transforms (apply_coeff_C_mat_CT / CT_mat_C of the reference)
+    def _sparse_mm(self, side, rows, mat3, R, K, M):
+        """jk_sparse_mm on a contiguous float64 [n, ., .] CUDA tensor."""
+        out = torch.empty((mat3.shape[0], R, M), dtype=torch.float64, device=mat3.device)
+        libjk.check(libjk.load().jk_sparse_mm(side, rows[0].data_ptr(), rows[1].data_ptr(), rows[2].data_ptr(),
+                                               mat3.shape[0], R, K, M, mat3.data_ptr(), out.data_ptr(),
+                                               torch.cuda.current_stream().cuda_stream), 'jk_sparse_mm')
+        return out
+
+    def _as3(self, mat, n1, n2):
+        m = torch.as_tensor(mat, dtype=torch.float64, device='cuda')
+        return m.reshape(-1, n1, n2).contiguous(), m.shape[:-2]
+
     def apply_coeff_C_mat_CT(self, mat):
+        """C mat C^T for user-basis matrices [..., nao, nao] (two sparse
+        products with the rows of C)."""
         if self.sorted_mol is None:
             self.build()
-        c = self._coeff
-        return torch.matmul(torch.matmul(c, mat), c.T)
+        ns, nu = self.sorted_mol.nao, self.sorted_mol.nao_user
+        m3, lead = self._as3(mat, nu, nu)
+        t = self._sparse_mm(0, self._c_rows, m3, nu, nu, ns)
+        return self._sparse_mm(1, self._c_rows, t, ns, nu, ns).reshape(lead + (ns, ns))
 
     def apply_coeff_CT_mat_C(self, mat):
+        """C^T mat C for sorted-basis matrices [..., nao_s, nao_s]."""
         if self.sorted_mol is None:
             self.build()
-        c = self._coeff
-        return torch.matmul(torch.matmul(c.T, mat), c)
+        ns, nu = self.sorted_mol.nao, self.sorted_mol.nao_user
+        m3, lead = self._as3(mat, ns, ns)
+        t = self._sparse_mm(0, self._ct_rows, m3, ns, ns, nu)
+        return self._sparse_mm(1, self._ct_rows, t, nu, ns, nu).reshape(lead + (nu, nu))
 
     def apply_coeff_C_mat(self, mat):
+        """C mat for user-basis row blocks [..., nao, m]."""
         if self.sorted_mol is None:
             self.build()
-        return torch.matmul(self._coeff, mat)
+        ns, nu = self.sorted_mol.nao, self.sorted_mol.nao_user
+        mat = torch.as_tensor(mat, dtype=torch.float64, device='cuda')
+        m = mat.shape[-1]
+        m3, lead = self._as3(mat, nu, m)
+        return self._sparse_mm(1, self._c_rows, m3, ns, nu, m).reshape(lead + (ns, m))
 
     # -- J/K in the sorted basis --------------------------------------------
     def _build(self, dms, hermi, with_j, with_k, stats=False, op=(0., 1., 1.)):

@@ -168,6 +168,20 @@ int jk_energy_grad(jk_opt *opt, const double *dm, int n_dm, int nao, double j_fa
                    double k_factor, double omega, double lr_factor, double sr_factor,
                    double *ejk, void *stream, jk_stats *stats);
 
+/* Products with the sparse map C between the user basis and the sorted
+ * basis, given as compressed rows S = (ptr[rows+1], idx, val) in device
+ * memory; replaces the dense C / C^T products of SortedGTO.apply_C_mat_CT
+ * and apply_CT_mat_C (gpu4pyscf/gto/mole.py:906-938).
+ *   side 0 (right): out[i][r][m] = sum_p in[i][r][idx[p]] val[p] over row m
+ *                   of S (S has M rows, idx < K); in [n][R][K]
+ *   side 1 (left):  out[i][r][m] = sum_p val[p] in[i][idx[p]][m] over row r
+ *                   of S (S has R rows, idx < K); in [n][K][M]
+ * out [n][R][M].  C D C^T is right then left with S = C (rows: sorted AOs);
+ * C^T V C right then left with S = C^T.  The index arrays are the
+ * caller's to keep in range.  Asynchronous on stream. */
+int jk_sparse_mm(int side, const int *ptr, const int *idx, const double *val, int n, int R, int K, int M,
+                 const double *in, double *out, void *stream);
+
 /* Autotuner (no counterpart in the reference, whose launch schemes are
  * fixed per class).  jk_opt_tune times, for every angular class (and
  * precision) the optimizer launches, each kernel family the class has

@@ -82,6 +82,44 @@ def test_diffuse_primitives_peeled(cart):
     assert abs(C.T @ vk_s @ C - vk0).max() < 1e-10
 
 
+def _sparse_emul(side, rows, a, R, K, M):
+    """The formulas of jk_sparse_mm in numpy (a: [n, ., .])."""
+    ptr, idx, val = rows
+    out = np.zeros((a.shape[0], R, M))
+    for r in range(R):
+        for m in range(M):
+            if side == 0:
+                p = slice(ptr[m], ptr[m + 1])
+                out[:, r, m] = a[:, r, idx[p]] @ val[p]
+            else:
+                p = slice(ptr[r], ptr[r + 1])
+                out[:, r, m] = np.einsum('p,np->n', val[p], a[:, idx[p], m])
+    return out
+
+
+@pytest.mark.parametrize('cart, cutoff', [(False, 0.), (True, 0.), (False, 0.3)])
+def test_sparse_transform_rows(cart, cutoff):
+    """The compressed rows of C and C^T with the sparse-product formulas of
+    jk_sparse_mm give C D C^T and C^T V C."""
+    extra = [[0, [10., .3], [1., .5], [.2, .4], [.05, .2]]]
+    mol = gto.M(atom='O 0 0 0.1174; H -0.757 0 -0.4696; H 0.757 0 -0.4696',
+                basis=('syn-def2-tzvp', extra), cart=cart)
+    sb = SortedBasis(mol, cutoff)
+    C = sb.coeff
+    ns, nu = C.shape
+    rng = np.random.default_rng(4)
+    D = rng.random((2, nu, nu))
+    V = rng.random((2, ns, ns))
+    rc, rt = sb.coeff_rows(), sb.coeff_rows(transpose=True)
+    assert rc[0][-1] == len(rc[2]) == np.count_nonzero(C) and rt[0][-1] == len(rt[2])
+    t = _sparse_emul(0, rc, D, nu, nu, ns)
+    ds = _sparse_emul(1, rc, t, ns, nu, ns)
+    assert abs(ds - C @ D @ C.T).max() < 1e-12
+    t = _sparse_emul(0, rt, V, ns, ns, nu)
+    vu = _sparse_emul(1, rt, t, nu, ns, nu)
+    assert abs(vu - C.T @ V @ C).max() < 1e-12
+
+
 def test_basis_parsing_forms():
     m1 = gto.M(atom='C 0 0 0', basis=('sto-3g', [[3, [1.4, 1.]]]))
     assert list(m1._bas[:, 1]) == [0, 0, 1, 3]
