@@ -26,11 +26,12 @@ from . import jk as jk_mod
 from ..lib import libjk
 
 
-def get_jk(mol, dm, hermi=1, vhfopt=None, with_j=True, with_k=True, omega=None, verbose=None):
+def get_jk(mol, dm, hermi=1, vhfopt=None, with_j=True, with_k=True, omega=None, lr_factor=None,
+           sr_factor=None, verbose=None):
     """J/K with the reference's module-level conventions: numpy input gives
     numpy output (gpu4pyscf/scf/hf.py:49-57)."""
     is_np = not isinstance(dm, torch.Tensor)
-    vj, vk = jk_mod.get_jk(mol, dm, hermi, vhfopt, with_j, with_k, omega)
+    vj, vk = jk_mod.get_jk(mol, dm, hermi, vhfopt, with_j, with_k, omega, lr_factor, sr_factor)
     if is_np:
         vj = vj.cpu().numpy() if vj is not None else None
         vk = vk.cpu().numpy() if vk is not None else None

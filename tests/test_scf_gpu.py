@@ -22,6 +22,27 @@ def test_int1e_vs_oracle():
     assert abs(H - href).max() < 1e-10
 
 
+def test_module_get_jk_numpy_in_numpy_out():
+    """hf.get_jk (gpu4pyscf/scf/hf.py:49-57): numpy input gives numpy output,
+    torch input torch output, the range-separation factors pass through."""
+    import torch
+    from gpu4pyscf_gb300.scf import hf, jk
+    mol = gto.M(atom=H2O, basis='syn-cc-pvdz')
+    rng = np.random.default_rng(8)
+    a = rng.random((mol.nao, mol.nao)) - .5
+    dm = a + a.T
+    vj, vk = hf.get_jk(mol, dm)
+    assert isinstance(vj, np.ndarray) and isinstance(vk, np.ndarray)
+    rj, rk = orc.get_jk(mol, dm, hermi=1)
+    assert abs(vj - rj).max() < 1e-10 and abs(vk - rk).max() < 1e-10
+    tj, tk = hf.get_jk(mol, torch.as_tensor(dm, device='cuda'))
+    assert isinstance(tj, torch.Tensor) and abs(tj.cpu().numpy() - rj).max() < 1e-10
+    _, k_lr = hf.get_jk(mol, dm, with_j=False, omega=.3, lr_factor=1., sr_factor=0.)
+    _, k_ref = jk.get_jk(mol, dm, hermi=1, with_j=False, omega=.3, lr_factor=1., sr_factor=0.)
+    assert isinstance(k_lr, np.ndarray) and abs(k_lr - k_ref.cpu().numpy()).max() < 1e-12
+    assert abs(k_lr - rk).max() > 1e-3      # the long-range K differs from the full one
+
+
 @pytest.mark.parametrize('basis', ['sto-3g', 'syn-cc-pvdz'])
 def test_rhf_energy_vs_oracle(basis):
     from gpu4pyscf_gb300.scf import hf
