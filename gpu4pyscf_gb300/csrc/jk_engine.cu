@@ -1250,6 +1250,7 @@ int jk_energy_grad(jk_opt *o, const double *dm, int n_dm, int nao, double j_fact
     if (npass < 0 || !std::isfinite(omega) || !std::isfinite(lr_factor) || !std::isfinite(sr_factor))
         return fail(JK_ERR_ARG, "jk_energy_grad: omega = 0 needs lr_factor == sr_factor");
     cudaStream_t st = (cudaStream_t)stream;
+    if (stats) std::memset(stats, 0, sizeof(*stats));
     CK(cudaMemsetAsync(ejk, 0, sizeof(double) * 3 * o->natm, st));
     if (npass == 0 || (j_factor == 0. && k_factor == 0.)) return 0;
     // weights of the density products (the reference's convention): 8-fold
@@ -1343,7 +1344,8 @@ int jk_energy_grad(jk_opt *o, const double *dm, int n_dm, int nao, double j_fact
             stats->quartets_fp64 += (int64_t)cnt[2 * q];
             stats->prim_quartets_fp64 += (int64_t)cnt[2 * q + 1];
         }
-        stats->kernel_launches = 4 + 2 + npass * (int)o->plan_classes.size();
+        // density maxima (2), bound, plan and scan, and the class launches
+        stats->kernel_launches = 3 + (o->nplan > 0 ? 2 : 0) + npass * (int)o->plan_classes.size();
         stats->n_classes = (int)o->plan_classes.size();
     }
     return 0;
